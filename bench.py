@@ -1,0 +1,347 @@
+#!/usr/bin/env python3
+"""Throughput of the fused D3Q19 stream-and-collide step on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--storage f32|f16|bf16|f64]
+    python bench.py --impl reference ...      # the CPU restatement on the host cores
+
+Workload: the LES cylinder at Re 300, 512 x 256 x 64 cells, cylinder r = 16 at
+(128, 128), inflow U = 0.08, free-slip z-walls, periodic y, sponge over the
+last 32 x-planes, seeded velocity noise +-1e-3 (synthetic; no dataset). A
+"step" is one quiet stream-collide pass over the whole lattice. The metric
+is GLUPS (giga lattice-cell updates per second; the reference prints MLUPS,
+bench.py:23 there). The population buffer (19 x 4 B x 8.4M = 637 MB in FP32)
+is larger than the 129 MB L2, so no flush is needed between steps.
+
+Prints one JSON line. ``value`` is device-timed (CUDA events on the launch
+stream, populations resident in HBM); ``e2e`` runs the public Solver API
+(step with report + monitors, a device-to-host read of the FP64 monitor sums
+every step); ``roofline`` is the bulk step kernel's algorithmic bytes over
+its event-timed duration against the measured HBM copy bandwidth.
+
+Under torchrun (N > 1) every rank runs an independent replica on its own GPU
+(the step does not shard: replicas only); rank 0 prints the line.
+"""
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "tack-lbm_gb300"))
+
+WORKLOAD = dict(nx=512, ny=256, nz=64, collision="les", reynolds=300.0, u0=0.08, diameter=32.0,
+                obstacle="cylinder", center=(128.0, 128.0, 32.0), vertical="slip", lateral="periodic",
+                sponge_planes=32, u_noise=1e-3, rho_sigma=0.0, seed=20240601)
+BYTES_PER_CELL = {"f32": 152, "f16": 76, "bf16": 76, "f64": 304}
+DTYPE = {"f32": "f32", "f16": "f16 storage, f32 arithmetic", "bf16": "bf16 storage, f32 arithmetic",
+         "f64": "f64"}
+
+
+def workload_config(storage):
+    w = WORKLOAD
+    return {"workload": f"LES cylinder Re 300, {w['nx']}x{w['ny']}x{w['nz']}, r 16, slip z, sponge 32",
+            "cells": w["nx"] * w["ny"] * w["nz"], "storage": storage, "collision": w["collision"],
+            "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas"}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """Samples nvidia-smi SM clocks and throttle reasons while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(n_gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        return world, rank, local, dist, torch
+    return 1, 0, 0, None, None
+
+
+def barrier(dist, torch):
+    if dist is not None:
+        dist.barrier()
+        torch.cuda.synchronize()
+
+
+def max_over_ranks(value, dist, torch):
+    if dist is None:
+        return value
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_solver(storage, device):
+    import lbm
+    w = WORKLOAD
+    return lbm.Solver(w["nx"], w["ny"], w["nz"], collision=w["collision"], obstacle=w["obstacle"],
+                      reynolds=w["reynolds"], u0=w["u0"], diameter=w["diameter"],
+                      device=f"cuda:{device}", lateral=w["lateral"], vertical=w["vertical"],
+                      storage=storage, obstacle_center=w["center"], sponge_planes=w["sponge_planes"],
+                      init="random", seed=w["seed"], rho_sigma=w["rho_sigma"], u_noise=w["u_noise"])
+
+
+def oracle_config():
+    from oracle import lbm_oracle as O
+    w = WORKLOAD
+    cx, cy, _ = w["center"]
+    return O.Config(w["nx"], w["ny"], w["nz"], collision=w["collision"],
+                    nu=w["u0"] * w["diameter"] / w["reynolds"], obstacle=w["obstacle"], ox=cx, oy=cy,
+                    r=w["diameter"] / 2, u0=w["u0"], sponge_start=w["nx"] - w["sponge_planes"],
+                    sponge_strength=1.0, lateral=w["lateral"], vertical=w["vertical"])
+
+
+def cpu_sample_step(f, cells):
+    from oracle import lbm_oracle as O
+    O.step(oracle_config(), f, cells=cells, dtype=np.float32)
+
+
+def cpu_baseline_single(f, target_s=12.0):
+    """The oracle step (float32 NumPy, one process) on a growing sample of z-planes."""
+    cfg_nxy = WORKLOAD["nx"] * WORKLOAD["ny"]
+    planes, elapsed = 1, 0.0
+    while True:
+        cells = np.arange(planes * cfg_nxy)
+        t0 = time.perf_counter()
+        cpu_sample_step(f, cells)
+        elapsed = time.perf_counter() - t0
+        if elapsed >= target_s / 4 or planes >= WORKLOAD["nz"]:
+            break
+        planes = min(WORKLOAD["nz"], planes * 4)
+    return {"value": cells.size / elapsed / 1e9, "unit": "GLUPS", "cores": 1, "kind": "port",
+            "sample": f"one step of {planes} z-plane(s) ({cells.size} cells) of the workload, "
+                      f"float32 NumPy oracle, {elapsed:.1f} s"}
+
+
+# ---------------------------------------------------------------------------
+# reference arm: the CPU restatement over all host cores
+
+def _worker(args):
+    shm_name, shape, lo, hi = args
+    from multiprocessing import shared_memory
+    shm = shared_memory.SharedMemory(name=shm_name)
+    try:
+        f = np.ndarray(shape, dtype=np.float32, buffer=shm.buf)
+        t0 = time.perf_counter()
+        cpu_sample_step(f, np.arange(lo, hi))
+        return time.perf_counter() - t0
+    finally:
+        shm.close()
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1 and rank != 0:
+        return 0
+    import multiprocessing as mp
+    from multiprocessing import shared_memory
+    from oracle import lbm_oracle as O
+    w = WORKLOAD
+    cfg = oracle_config()
+    f0 = O.init_random(cfg, w["rho_sigma"], w["u_noise"], w["seed"]).astype(np.float32)
+    shm = shared_memory.SharedMemory(create=True, size=f0.nbytes)
+    try:
+        f = np.ndarray(f0.shape, dtype=np.float32, buffer=shm.buf)
+        f[...] = f0
+        del f0
+        cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+        nxy = w["nx"] * w["ny"]
+        # each step: one oracle pass over a sample of z-planes, split across all cores
+        planes = max(1, min(w["nz"], int(os.environ.get("LBM_REF_PLANES", "2"))))
+        sample = planes * nxy
+        bounds = np.linspace(0, sample, cores + 1).astype(int)
+        jobs = [(shm.name, f.shape, int(bounds[i]), int(bounds[i + 1])) for i in range(cores)]
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(cores) as pool:
+            for _ in range(args.warmup):
+                pool.map(_worker, jobs)
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                pool.map(_worker, jobs)
+            dt = time.perf_counter() - t0
+    finally:
+        shm.close()
+        shm.unlink()
+    value = sample * args.steps / dt / 1e9
+    desc = (f"one float32 NumPy oracle pass over {planes} z-plane(s) ({sample} cells) of the workload "
+            f"per step, split over {cores} processes")
+    line = {"impl": "reference", "metric": "GLUPS", "value": value, "unit": "GLUPS", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": workload_config("f32"),
+            "cpu_baseline": {"value": value, "unit": "GLUPS", "cores": cores, "kind": "port", "sample": desc},
+            "e2e": {"value": value, "unit": "GLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16", "f64"])
+    ap.add_argument("--e2e-steps", type=int, default=100)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference(args)
+
+    world, rank, local, dist, torch = dist_setup(args.gpus)
+    import lbm_native as N
+    s = make_solver(args.storage, local)
+    steps = min(args.steps, 4096)
+    for _ in range(args.warmup):
+        s.step()
+    s.sync()
+    s._h.call("lbm_timing", 1)
+    barrier(dist, torch)
+    with Clocks(local) as clocks:
+        t0 = time.perf_counter()
+        s.run(steps)
+        s.sync()
+        wall = time.perf_counter() - t0
+    barrier(dist, torch)
+    t = (ctypes.c_double * 7)()
+    s._h.call("lbm_timing_read", t)
+    s._h.call("lbm_timing", 0)
+    span_ms = max_over_ranks(t[6], dist, torch)
+    cells = s.lat.n
+    value = world * cells * steps / (span_ms * 1e-3) / 1e9
+    bulk_ms = t[0] / max(t[1], 1)
+    generic_ms = t[3] / max(t[4], 1) if t[4] else 0.0
+    solid = int(s.mask().sum())
+    bytes_cell = BYTES_PER_CELL[args.storage]
+    # the bulk kernel's cells are all fluid; it moves bytes_cell bytes per cell
+    bulk_bytes = bytes_cell * t[2]
+    achieved = bulk_bytes / (bulk_ms * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    step_bytes = bytes_cell * (cells - solid)
+
+    # end to end through the public API: a report step and monitors() every step
+    e2e_steps = max(1, args.e2e_steps)
+    for _ in range(3):
+        s.step(report=True)
+        s.monitors(1)
+    barrier(dist, torch)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        s.step(report=True)
+        m = s.monitors(1)
+    e2e_wall = max_over_ranks(time.perf_counter() - t0, dist, torch)
+    e2e_value = world * cells * e2e_steps / e2e_wall / 1e9
+    finite = all(np.isfinite(v) for v in m.values())
+
+    line = {
+        "metric": "GLUPS", "value": value, "unit": "GLUPS", "n_gpus": world, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": span_ms / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[args.storage], "data": "synthetic",
+        "config": workload_config(args.storage),
+        "e2e": {"value": e2e_value, "unit": "GLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 64,
+                "api": "Solver.step(report=True) + Solver.monitors(1) per step",
+                "ms_per_step": e2e_wall / e2e_steps * 1e3},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
+                     "traffic": None, "kernel": "bulk_kernel", "bytes_per_cell": bytes_cell,
+                     "cells_per_launch": int(t[2]), "ms_per_launch": bulk_ms},
+        "step_roofline": {"achieved": step_bytes / (span_ms / steps * 1e-3) / 1e9,
+                          "frac": step_bytes / (span_ms / steps * 1e-3) / 1e9 / peak,
+                          "generic_ms_per_launch": generic_ms, "generic_cells": int(t[5])},
+        "gpu_launches": int(t[1] + t[4]),
+        "clocks": clocks.summary(),
+        "monitors_finite": bool(finite),
+        "wall_s": wall,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        f = s.populations(np.float32)
+        line["cpu_baseline"] = cpu_baseline_single(f)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

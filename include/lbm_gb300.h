@@ -1,0 +1,198 @@
+/*
+ * lbm_gb300.h - C ABI of the GB300 (sm_103a) D3Q19 stream-and-collide solver.
+ *
+ * This is the boundary a host binding (ctypes, cuda-python, cffi) calls in
+ * place of tack-lbm's Tack-compiled kernels and its Solver plumbing. It takes
+ * plain pointers and sizes only; every function returns an lbm_status and
+ * never throws. lbm_last_error() gives a message for the last failure on the
+ * calling thread.
+ *
+ * Populations live on the GPU in one structure-of-arrays buffer that is
+ * updated in place (AA pattern), so there is no A/B pair to swap. Host-side
+ * exchange of populations always uses the reference layout f[q*n + idx],
+ * idx = (z*ny + y)*nx + x (lbm.py:397-402, lbm.py:426), whatever storage
+ * precision is used on the device.
+ *
+ * Reference interfaces replaced (paths inside the tack-lbm project):
+ *   lbm_create/lbm_destroy  Solver.__init__ buffers and composition (lbm.py:551-584)
+ *   lbm_init                lbm_init kernel (lbm.py:383-394)
+ *   lbm_step                Solver.step -> lbm_step kernel + buffer swap (lbm.py:639-647, 397-513)
+ *   lbm_monitors            Solver.monitors (lbm.py:649-661)
+ *   lbm_field               ManagedArray fields (lbm.py:525-541, 567)
+ *   lbm_set_physics         Solver.set_physics (lbm.py:613-616)
+ *   lbm_set_obstacle        Solver.set_obstacle (lbm.py:628-637)
+ *   lbm_set_actuation       Solver.set_actuation / omega_rot (lbm.py:618-624)
+ */
+#ifndef LBM_GB300_H
+#define LBM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum lbm_status {
+    LBM_OK = 0,
+    LBM_ERR_ARG = 1,        /* bad argument: unknown model/obstacle (the reference's KeyError), bad size */
+    LBM_ERR_CUDA = 2,       /* a CUDA call failed (the reference's RuntimeError, lbm.py:533-534) */
+    LBM_ERR_NONFINITE = 3,  /* a monitor sum is NaN or Inf: the run diverged (collision_check.py:19) */
+    LBM_ERR_STATE = 4       /* call not valid in the solver's current state */
+} lbm_status;
+
+/* collision models: the COLLISIONS registry (lbm.py:544) */
+enum { LBM_BGK = 0, LBM_TRT = 1, LBM_LES = 2 };
+/* obstacles (lbm.py:144-227); LBM_NO_OBSTACLE has no solid cell */
+enum { LBM_NO_OBSTACLE = 0, LBM_CYLINDER = 1, LBM_SPHERE = 2, LBM_BOX = 3 };
+/* y boundaries: PeriodicY / SlipY (lbm.py:342-369); LID adds a moving no-slip top wall (new) */
+enum { LBM_PERIODIC = 0, LBM_SLIP = 1, LBM_LID = 2 };
+/* population storage on the device: FP32, FP16/BF16 deviations f - w_q, FP64 (oracle runs) */
+enum { LBM_F32 = 0, LBM_F16 = 1, LBM_BF16 = 2, LBM_F64 = 3 };
+/* diagnostic fields, in the reference's FIELDS order (lbm.py:545) */
+enum {
+    LBM_UX = 0, LBM_UY, LBM_UZ, LBM_P, LBM_VMAG, LBM_R_RHO, LBM_R_UX, LBM_R_UY, LBM_R_UZ,
+    LBM_R_KE, LBM_FX, LBM_FY, LBM_FZ, LBM_NUM_FIELDS
+};
+/* lbm_monitors output order: the keys of Solver.monitors (lbm.py:655-660) */
+enum {
+    LBM_MON_CONTINUITY = 0, LBM_MON_MOMENTUM_X, LBM_MON_MOMENTUM_Y, LBM_MON_MOMENTUM_Z,
+    LBM_MON_ENERGY, LBM_MON_DRAG, LBM_MON_LIFT, LBM_NUM_MONITORS
+};
+/* where a host/device buffer lives */
+enum { LBM_HOST = 0, LBM_DEVICE = 1 };
+
+typedef struct lbm_config {
+    int32_t nx, ny, nz;          /* lattice (lbm.py:42-44) */
+    int32_t collision;           /* LBM_BGK | LBM_TRT | LBM_LES */
+    int32_t obstacle;            /* LBM_NO_OBSTACLE | LBM_CYLINDER | LBM_SPHERE | LBM_BOX */
+    int32_t lateral;             /* y: LBM_PERIODIC | LBM_SLIP | LBM_LID */
+    int32_t vertical;            /* z: LBM_PERIODIC | LBM_SLIP (the reference is periodic, lbm.py:415) */
+    int32_t storage;             /* LBM_F32 | LBM_F16 | LBM_BF16 | LBM_F64 */
+    double nu;                   /* kinematic viscosity, tau0 = 3 nu + 1/2 (lbm.py:63, 110, 131) */
+    double cs;                   /* Smagorinsky constant for TRT/LES (reference: 0.16, lbm.py:107, 128) */
+    double magic;                /* TRT magic parameter (reference: 0.1875, lbm.py:106) */
+    double ox, oy, oz;           /* obstacle centre (lbm.py:630-637) */
+    double r;                    /* cylinder/sphere radius */
+    double hx, hy, hz;           /* box half sizes */
+    double u0;                   /* inflow / sponge target velocity (lbm.py:372-380) */
+    double sponge_start;         /* first sponge plane, reference 0.75 nx (lbm.py:561) */
+    double sponge_strength;      /* reference 1.0 */
+    double u_lid;                /* x velocity of the LBM_LID top wall */
+    double omega_rot;            /* cylinder surface speed (lbm.py:618-620) */
+    int32_t device;              /* CUDA device ordinal */
+    int32_t reserved;
+} lbm_config;
+
+typedef struct lbm_solver lbm_solver;
+
+/* Create a solver: validate cfg, allocate the population buffer (device
+ * memory) and the 13 diagnostic fields (CUDA managed memory, zeroed, stable for
+ * the handle's lifetime so Conduit/NumPy may alias them). Populations are
+ * undefined until lbm_init / lbm_init_random / lbm_set_populations.
+ * Replaces Solver.__init__ allocation and composition (lbm.py:551-584). */
+lbm_status lbm_create(const lbm_config *cfg, lbm_solver **out);
+lbm_status lbm_destroy(lbm_solver *s);
+
+/* Equilibrium at rho = 1, u = (u0*fluid, seed_amp*u0*fluid*sin(2 pi x/nx)*cos(2 pi z/nz), 0)
+ * (lbm_init, lbm.py:383-394). Resets the step counter. */
+lbm_status lbm_init(lbm_solver *s, double seed_amp);
+
+/* Equilibrium at rho = 1 + rho_sigma*N(0,1), u = (u0, 0, 0) + U(-u_noise, u_noise)^3 in
+ * fluid cells, rest elsewhere, from a counter-based generator keyed by seed.
+ * (No reference counterpart: the configurations' seeded start states.) */
+lbm_status lbm_init_random(lbm_solver *s, double rho_sigma, double u_noise, uint64_t seed);
+
+/* One step of the fused stream-collide kernel; report != 0 also writes the 13
+ * fields and the FP64 monitor sums (lbm_step with Report, lbm.py:493-513).
+ * Asynchronous on `stream` (a cudaStream_t; NULL = the legacy default stream).
+ * Replaces Solver.step (lbm.py:639-647). */
+lbm_status lbm_step(lbm_solver *s, int32_t report, void *stream);
+
+/* `count` quiet steps, the last one a report step when report_last != 0. */
+lbm_status lbm_run(lbm_solver *s, int32_t count, int32_t report_last, void *stream);
+
+/* Synchronise and return the monitors of the last report step, in
+ * LBM_MON_* order: residuals sqrt(sum/n)/max(interval,1) and drag/lift
+ * sum(f)/(0.5 u0^2 diameter nz) (Solver.monitors, lbm.py:649-661). The sums
+ * are reduced on the GPU in FP64; no field page is touched by the host.
+ * Returns LBM_ERR_NONFINITE (with the values filled in) when a sum is not finite. */
+lbm_status lbm_monitors(lbm_solver *s, int32_t interval, double diameter, double out[7]);
+
+/* The raw FP64 sums of the last report step: r_rho, r_ux, r_uy, r_uz, r_ke, fx, fy, fz. */
+lbm_status lbm_field_sums(lbm_solver *s, double out[8]);
+
+/* Managed pointer to field `id` (n floats), valid until lbm_destroy (lbm.py:525-541). */
+lbm_status lbm_field(lbm_solver *s, int32_t id, float **ptr);
+
+/* Change collision model and viscosity; cs < 0 keeps the current constant (lbm.py:613-616). */
+lbm_status lbm_set_physics(lbm_solver *s, int32_t collision, double nu, double cs);
+
+/* Change the obstacle: geo = {ox, oy, oz, r, hx, hy, hz}. The populations are
+ * carried over as the reference does (lbm.py:628-637). */
+lbm_status lbm_set_obstacle(lbm_solver *s, int32_t kind, const double geo[7]);
+
+/* Cylinder surface speed, stream-ordered with the steps (lbm.py:618-624). */
+lbm_status lbm_set_actuation(lbm_solver *s, double omega_rot);
+lbm_status lbm_get_actuation(lbm_solver *s, double *omega_rot);
+
+/* Sponge start plane and strength (Flow, lbm.py:372-380). */
+lbm_status lbm_set_sponge(lbm_solver *s, double start, double strength);
+
+/* Copy populations in/out in the reference layout f[q*n + idx] (19*n values).
+ * dtype: LBM_F32 or LBM_F64 values; where: LBM_HOST or LBM_DEVICE pointer.
+ * lbm_set_populations leaves the solver at the start of a step; solid cells
+ * read back as w_q, the value every reference step gives them (lbm.py:449-456). */
+lbm_status lbm_set_populations(lbm_solver *s, const void *f, int32_t dtype, int32_t where);
+lbm_status lbm_get_populations(lbm_solver *s, void *f, int32_t dtype, int32_t where);
+
+/* Output grid: the fields ux, uy, uz, p, vmag subsampled by `stride` along each
+ * axis, (d + stride - 1)/stride points per axis, in managed memory
+ * (lbm.py:574-581). stride 1 aliases the full-resolution fields. */
+lbm_status lbm_set_output_stride(lbm_solver *s, int32_t stride);
+/* Managed pointer to output field `id` (LBM_UX .. LBM_VMAG) and its point count. */
+lbm_status lbm_output(lbm_solver *s, int32_t id, float **ptr, int64_t *count);
+/* Refresh the output fields from the full-resolution ones: the coarsen kernel
+ * (lbm.py:516-522) for every output field (Solver.update_output, lbm.py:606-611). */
+lbm_status lbm_update_output(lbm_solver *s, void *stream);
+
+/* Overwrite one diagnostic field from a buffer of n floats (host or managed). */
+lbm_status lbm_set_field(lbm_solver *s, int32_t id, const float *host);
+
+/* Solid mask (1 inside the obstacle) as n bytes on the host. */
+lbm_status lbm_mask(lbm_solver *s, uint8_t *host_out);
+
+/* Number of steps taken since the last init / set_populations. */
+lbm_status lbm_step_count(lbm_solver *s, int64_t *count);
+
+/* Device bytes held by the solver (populations + fields + scratch). */
+lbm_status lbm_memory(lbm_solver *s, int64_t *bytes);
+
+/* A zeroed CUDA managed float array of `count` elements, readable from the
+ * host and the GPU (ManagedArray, lbm.py:525-541); free with lbm_managed_free. */
+lbm_status lbm_managed_alloc(int64_t count, float **ptr);
+lbm_status lbm_managed_free(float *ptr);
+
+/* Kernel timing: when enabled, every step records CUDA events around the bulk
+ * and generic step kernels on the launching stream. lbm_timing_read
+ * synchronises and returns {bulk ms total, bulk launches, bulk cells per
+ * launch, generic ms total, generic launches, generic cells per launch, ms
+ * from the first timed step's start to the last one's end} since the last
+ * enable (at most 4096 steps are timed). (No reference counterpart:
+ * measurement support.) */
+lbm_status lbm_timing(lbm_solver *s, int32_t enable);
+lbm_status lbm_timing_read(lbm_solver *s, double out[7]);
+
+/* Synchronise the solver's device work (tack.sync, lbm.py:651). */
+lbm_status lbm_sync(lbm_solver *s);
+
+/* Message of the last error on this thread ("" when none). */
+const char *lbm_last_error(void);
+
+/* ABI version: bump when a signature or struct changes. */
+int32_t lbm_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LBM_GB300_H */

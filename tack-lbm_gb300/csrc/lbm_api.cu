@@ -1,0 +1,742 @@
+// lbm_api.cu - the C ABI (include/lbm_gb300.h): solver handles, buffers, dispatch.
+//
+// One solver owns: the in-place AA population buffer (device memory), the 13
+// diagnostic fields (CUDA managed memory, as the reference's ManagedArray,
+// lbm.py:525-541), the per-block FP64 partial sums of report steps and the
+// block classification (bulk vs generic) of its geometry.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "lbm_device.cuh"
+#include "lbm_host.h"
+
+using lbmh::Ctx;
+
+struct lbm_solver {
+  Ctx c;
+  int64_t bytes = 0;
+  int64_t steps = 0;
+  bool reported = false;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+lbm_status fail(lbm_status s, const std::string &msg) {
+  g_err = msg;
+  return s;
+}
+
+#define LBM_CUDA(call)                                                                         \
+  do {                                                                                         \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess)                                                                     \
+      return fail(LBM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));           \
+  } while (0)
+
+size_t storage_bytes(int storage) {
+  switch (storage) {
+    case LBM_F16: return sizeof(__half);
+    case LBM_BF16: return sizeof(__nv_bfloat16);
+    case LBM_F64: return sizeof(double);
+    default: return sizeof(float);
+  }
+}
+
+lbm_status validate(const lbm_config &g) {
+  if (g.nx < 1 || g.ny < 1 || g.nz < 1) return fail(LBM_ERR_ARG, "lattice sizes must be >= 1");
+  const int64_t n = (int64_t)g.nx * g.ny * g.nz;
+  if (n > 2147483647LL) return fail(LBM_ERR_ARG, "more than 2^31-1 cells");
+  if ((g.ny + lbmk::BY - 1) / lbmk::BY > 65535 || g.nz > 65535)
+    return fail(LBM_ERR_ARG, "ny/4 and nz must be <= 65535");
+  if (g.collision < LBM_BGK || g.collision > LBM_LES)
+    return fail(LBM_ERR_ARG, "unknown collision model (bgk=0, trt=1, les=2)");
+  if (g.obstacle < LBM_NO_OBSTACLE || g.obstacle > LBM_BOX)
+    return fail(LBM_ERR_ARG, "unknown obstacle (none=0, cylinder=1, sphere=2, box=3)");
+  if (g.lateral < LBM_PERIODIC || g.lateral > LBM_LID)
+    return fail(LBM_ERR_ARG, "unknown lateral policy (periodic=0, slip=1, lid=2)");
+  if (g.vertical != LBM_PERIODIC && g.vertical != LBM_SLIP)
+    return fail(LBM_ERR_ARG, "unknown vertical policy (periodic=0, slip=1)");
+  if (g.storage < LBM_F32 || g.storage > LBM_F64)
+    return fail(LBM_ERR_ARG, "unknown storage (f32=0, f16=1, bf16=2, f64=3)");
+  if (!(std::isfinite(g.nu) && g.nu > 0.0)) return fail(LBM_ERR_ARG, "nu must be finite and > 0");
+  if (!(std::isfinite(g.cs) && g.cs >= 0.0)) return fail(LBM_ERR_ARG, "cs must be finite and >= 0");
+  const double vals[] = {g.magic, g.ox, g.oy, g.oz, g.r, g.hx, g.hy, g.hz, g.u0,
+                         g.sponge_start, g.sponge_strength, g.u_lid, g.omega_rot};
+  for (double v : vals)
+    if (!std::isfinite(v)) return fail(LBM_ERR_ARG, "configuration values must be finite");
+  return LBM_OK;
+}
+
+// Cells that may be solid or have a solid neighbour lie in [lo, hi] along each axis.
+struct Range {
+  int64_t lo, hi;
+};
+
+void obstacle_box(const lbm_config &g, Range r[3], bool &any) {
+  double c[3] = {g.ox, g.oy, g.oz}, h[3] = {0, 0, 0};
+  any = true;
+  if (g.obstacle == LBM_CYLINDER || g.obstacle == LBM_SPHERE) {
+    h[0] = h[1] = h[2] = g.r;
+    if (!(g.r > 0)) any = false;
+  } else if (g.obstacle == LBM_BOX) {
+    h[0] = g.hx;
+    h[1] = g.hy;
+    h[2] = g.hz;
+    if (!(g.hx > 0 && g.hy > 0 && g.hz > 0)) any = false;
+  } else {
+    any = false;
+  }
+  const int64_t dims[3] = {g.nx, g.ny, g.nz};
+  for (int k = 0; k < 3; ++k) {
+    if (k == 2 && g.obstacle == LBM_CYLINDER) {
+      r[k] = {0, dims[k] - 1};
+      continue;
+    }
+    const double lo = std::floor(c[k] - h[k]) - 2.0, hi = std::ceil(c[k] + h[k]) + 2.0;
+    r[k].lo = (int64_t)std::max(lo, -1e15);
+    r[k].hi = (int64_t)std::min(hi, 1e15);
+    const bool periodic = k == 0 || (k == 1 && g.lateral == LBM_PERIODIC) ||
+                          (k == 2 && g.vertical == LBM_PERIODIC);
+    // a neighbour across a periodic boundary: widen to the whole axis
+    if (periodic && (r[k].lo <= 0 || r[k].hi >= dims[k] - 1)) r[k] = {0, dims[k] - 1};
+    if (r[k].hi < 0 || r[k].lo > dims[k] - 1) any = false;
+  }
+}
+
+lbm_status classify_blocks(lbm_solver *s) {
+  Ctx &c = s->c;
+  const lbm_config &g = c.cfg;
+  Range box[3];
+  bool any;
+  obstacle_box(g, box, any);
+  std::vector<uint8_t> flag((size_t)c.nblocks, 0);
+  std::vector<int> list;
+  const int last_by = (g.ny - 1) / lbmk::BY;
+  for (int z = 0; z < g.nz; ++z)
+    for (int by = 0; by < c.gy; ++by)
+      for (int bx = 0; bx < c.gx; ++bx) {
+        bool sp = false;
+        if (g.lateral != LBM_PERIODIC && (by == 0 || by == last_by)) sp = true;
+        if (g.vertical != LBM_PERIODIC && (z == 0 || z == g.nz - 1)) sp = true;
+        if (any) {
+          const int64_t x0 = (int64_t)bx * lbmk::BX, x1 = x0 + lbmk::BX - 1;
+          const int64_t y0 = (int64_t)by * lbmk::BY, y1 = y0 + lbmk::BY - 1;
+          if (x1 >= box[0].lo && x0 <= box[0].hi && y1 >= box[1].lo && y0 <= box[1].hi &&
+              z >= box[2].lo && z <= box[2].hi)
+            sp = true;
+        }
+        if (sp) {
+          const int bid = (z * c.gy + by) * c.gx + bx;
+          flag[(size_t)bid] = 1;
+          list.push_back(bid);
+        }
+      }
+  if (c.special) cudaFree(c.special);
+  if (c.special_list) cudaFree(c.special_list);
+  c.special = nullptr;
+  c.special_list = nullptr;
+  LBM_CUDA(cudaMalloc(&c.special, flag.size()));
+  LBM_CUDA(cudaMemcpy(c.special, flag.data(), flag.size(), cudaMemcpyHostToDevice));
+  c.nspecial = (int)list.size();
+  LBM_CUDA(cudaMalloc(&c.special_list, std::max<size_t>(1, list.size()) * sizeof(int)));
+  if (!list.empty())
+    LBM_CUDA(cudaMemcpy(c.special_list, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice));
+  return LBM_OK;
+}
+
+cudaError_t dispatch_step(const Ctx &c, bool report, cudaStream_t st) {
+  switch (c.cfg.storage) {
+    case LBM_F16: return lbmh::launch_step<__half>(c, report, st);
+    case LBM_BF16: return lbmh::launch_step<__nv_bfloat16>(c, report, st);
+    case LBM_F64: return lbmh::launch_step<double>(c, report, st);
+    default: return lbmh::launch_step<float>(c, report, st);
+  }
+}
+
+cudaError_t dispatch_init(const Ctx &c, double seed_amp, cudaStream_t st) {
+  switch (c.cfg.storage) {
+    case LBM_F16: return lbmh::launch_init<__half>(c, seed_amp, st);
+    case LBM_BF16: return lbmh::launch_init<__nv_bfloat16>(c, seed_amp, st);
+    case LBM_F64: return lbmh::launch_init<double>(c, seed_amp, st);
+    default: return lbmh::launch_init<float>(c, seed_amp, st);
+  }
+}
+
+cudaError_t dispatch_init_random(const Ctx &c, double rs, double un, uint64_t seed, cudaStream_t st) {
+  switch (c.cfg.storage) {
+    case LBM_F16: return lbmh::launch_init_random<__half>(c, rs, un, seed, st);
+    case LBM_BF16: return lbmh::launch_init_random<__nv_bfloat16>(c, rs, un, seed, st);
+    case LBM_F64: return lbmh::launch_init_random<double>(c, rs, un, seed, st);
+    default: return lbmh::launch_init_random<float>(c, rs, un, seed, st);
+  }
+}
+
+cudaError_t dispatch_import(const Ctx &c, const void *src, int dtype, cudaStream_t st) {
+  switch (c.cfg.storage) {
+    case LBM_F16: return lbmh::launch_import<__half>(c, src, dtype, st);
+    case LBM_BF16: return lbmh::launch_import<__nv_bfloat16>(c, src, dtype, st);
+    case LBM_F64: return lbmh::launch_import<double>(c, src, dtype, st);
+    default: return lbmh::launch_import<float>(c, src, dtype, st);
+  }
+}
+
+cudaError_t dispatch_export(const Ctx &c, void *dst, int dtype, cudaStream_t st) {
+  switch (c.cfg.storage) {
+    case LBM_F16: return lbmh::launch_export<__half>(c, dst, dtype, st);
+    case LBM_BF16: return lbmh::launch_export<__nv_bfloat16>(c, dst, dtype, st);
+    case LBM_F64: return lbmh::launch_export<double>(c, dst, dtype, st);
+    default: return lbmh::launch_export<float>(c, dst, dtype, st);
+  }
+}
+
+void release_output(Ctx &c) {
+  if (c.out_stride > 1)
+    for (int k = 0; k < 5; ++k) cudaFree(c.out[k]);
+  for (int k = 0; k < 5; ++k) c.out[k] = c.fld[k];
+  c.out_stride = 1;
+  c.out_dims[0] = c.cfg.nx;
+  c.out_dims[1] = c.cfg.ny;
+  c.out_dims[2] = c.cfg.nz;
+}
+
+void release_timing(Ctx &c) {
+  if (c.ev) {
+    for (int k = 0; k < 3 * c.ev_cap; ++k) cudaEventDestroy(c.ev[k]);
+    delete[] c.ev;
+  }
+  c.ev = nullptr;
+  c.ev_cap = c.ev_used = 0;
+}
+
+void release(lbm_solver *s) {
+  Ctx &c = s->c;
+  release_timing(c);
+  release_output(c);
+  cudaFree(c.F);
+  for (int k = 0; k < LBM_NUM_FIELDS; ++k) cudaFree(c.fld[k]);
+  cudaFree(c.partials);
+  cudaFree(c.stage);
+  cudaFree(c.sums);
+  cudaFree(c.special);
+  cudaFree(c.special_list);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// FP64 reduction of the per-block partial sums, in a fixed order (deterministic).
+
+namespace lbmh {
+
+__global__ void finalize_stage(const double *partials, int64_t nb, double *stage) {
+  __shared__ double sm[256][lbmk::NSUM];
+  const int64_t chunk = (nb + gridDim.x - 1) / gridDim.x;
+  const int64_t b0 = (int64_t)blockIdx.x * chunk;
+  const int64_t b1 = b0 + chunk < nb ? b0 + chunk : nb;
+  double acc[lbmk::NSUM] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int64_t b = b0 + threadIdx.x; b < b1; b += blockDim.x)
+    for (int k = 0; k < lbmk::NSUM; ++k) acc[k] += partials[b * lbmk::NSUM + k];
+  for (int k = 0; k < lbmk::NSUM; ++k) sm[threadIdx.x][k] = acc[k];
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+      for (int k = 0; k < lbmk::NSUM; ++k) sm[threadIdx.x][k] += sm[threadIdx.x + w][k];
+    __syncthreads();
+  }
+  if (threadIdx.x < lbmk::NSUM) stage[blockIdx.x * lbmk::NSUM + threadIdx.x] = sm[0][threadIdx.x];
+}
+
+__global__ void finalize_last(const double *stage, int g, double *sums) {
+  if (threadIdx.x < lbmk::NSUM) {
+    double s = 0.0;
+    for (int i = 0; i < g; ++i) s += stage[i * lbmk::NSUM + threadIdx.x];
+    sums[threadIdx.x] = s;
+  }
+}
+
+cudaError_t launch_finalize(const Ctx &c, cudaStream_t st) {
+  finalize_stage<<<FINALIZE_BLOCKS, 256, 0, st>>>(c.partials, c.nblocks, c.stage);
+  finalize_last<<<1, 32, 0, st>>>(c.stage, FINALIZE_BLOCKS, c.sums);
+  return cudaGetLastError();
+}
+
+__global__ void mask_kernel(lbmk::Geo geo, int nx, int ny, int n, uint8_t *out) {
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    int x, y, z;
+    lbmk::decode(idx, nx, ny, x, y, z);
+    out[idx] = lbmk::solid(geo, x, y, z) ? 1 : 0;
+  }
+}
+
+// coarsen (lbm.py:516-522): dst[(k*my + j)*mx + i] = src[((k*s)*ny + j*s)*nx + i*s] for 5 fields
+struct CoarsenArgs {
+  const float *src[5];
+  float *dst[5];
+};
+
+__global__ void coarsen_kernel(CoarsenArgs a, int nx, int ny, int s, int mx, int my, int m) {
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < m; idx += gridDim.x * blockDim.x) {
+    const int i = idx % mx, j = (idx / mx) % my, k = idx / (mx * my);
+    const int src = ((k * s) * ny + j * s) * nx + i * s;
+#pragma unroll
+    for (int f = 0; f < 5; ++f) a.dst[f][idx] = a.src[f][src];
+  }
+}
+
+cudaError_t launch_coarsen(const Ctx &c, cudaStream_t st) {
+  if (c.out_stride <= 1) return cudaSuccess;
+  CoarsenArgs a;
+  for (int f = 0; f < 5; ++f) {
+    a.src[f] = c.fld[f];
+    a.dst[f] = c.out[f];
+  }
+  const int m = c.out_dims[0] * c.out_dims[1] * c.out_dims[2];
+  coarsen_kernel<<<lbmk::cell_grid(m), 256, 0, st>>>(a, c.cfg.nx, c.cfg.ny, c.out_stride, c.out_dims[0],
+                                                     c.out_dims[1], m);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mask(const Ctx &c, uint8_t *dst, cudaStream_t st) {
+  mask_kernel<<<lbmk::cell_grid(c.n), 256, 0, st>>>(lbmk::make_geo(c.cfg), c.cfg.nx, c.cfg.ny, (int)c.n, dst);
+  return cudaGetLastError();
+}
+
+}  // namespace lbmh
+
+// ---------------------------------------------------------------------------
+// C ABI
+
+extern "C" {
+
+int32_t lbm_abi_version(void) { return 1; }
+
+const char *lbm_last_error(void) { return g_err.c_str(); }
+
+lbm_status lbm_create(const lbm_config *cfg, lbm_solver **out) {
+  if (!cfg || !out) return fail(LBM_ERR_ARG, "null argument");
+  *out = nullptr;
+  lbm_status st = validate(*cfg);
+  if (st != LBM_OK) return st;
+  LBM_CUDA(cudaSetDevice(cfg->device));
+  lbm_solver *s = new (std::nothrow) lbm_solver();
+  if (!s) return fail(LBM_ERR_ARG, "out of host memory");
+  Ctx &c = s->c;
+  c.cfg = *cfg;
+  c.n = (int64_t)cfg->nx * cfg->ny * cfg->nz;
+  c.gx = (cfg->nx + lbmk::BX - 1) / lbmk::BX;
+  c.gy = (cfg->ny + lbmk::BY - 1) / lbmk::BY;
+  c.nblocks = (int64_t)c.gx * c.gy * cfg->nz;
+  c.odd_next = 1;
+  c.omega_rot = cfg->omega_rot;
+  auto bail = [&](lbm_status e) {
+    release(s);
+    delete s;
+    return e;
+  };
+  const size_t fbytes = (size_t)19 * (size_t)c.n * storage_bytes(cfg->storage);
+  cudaError_t e = cudaMalloc(&c.F, fbytes);
+  if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("population buffer: ") + cudaGetErrorString(e)));
+  s->bytes += (int64_t)fbytes;
+  for (int k = 0; k < LBM_NUM_FIELDS; ++k) {
+    e = cudaMallocManaged(&c.fld[k], (size_t)c.n * sizeof(float), cudaMemAttachGlobal);
+    if (e == cudaSuccess) e = cudaMemset(c.fld[k], 0, (size_t)c.n * sizeof(float));
+    if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("cudaMallocManaged: ") + cudaGetErrorString(e)));
+    s->bytes += c.n * (int64_t)sizeof(float);
+  }
+  e = cudaMalloc(&c.partials, (size_t)c.nblocks * lbmk::NSUM * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&c.stage, lbmh::FINALIZE_BLOCKS * lbmk::NSUM * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&c.sums, lbmk::NSUM * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemset(c.sums, 0, lbmk::NSUM * sizeof(double));
+  if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("scratch: ") + cudaGetErrorString(e)));
+  s->bytes += (c.nblocks + lbmh::FINALIZE_BLOCKS + 1) * lbmk::NSUM * (int64_t)sizeof(double);
+  st = classify_blocks(s);
+  if (st != LBM_OK) return bail(st);
+  s->bytes += c.nblocks + (int64_t)c.nspecial * 4;
+  release_output(c);
+  e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("create: ") + cudaGetErrorString(e)));
+  *out = s;
+  return LBM_OK;
+}
+
+lbm_status lbm_destroy(lbm_solver *s) {
+  if (!s) return LBM_OK;
+  cudaSetDevice(s->c.cfg.device);
+  cudaDeviceSynchronize();
+  release(s);
+  delete s;
+  return LBM_OK;
+}
+
+#define LBM_HANDLE(s)                                        \
+  do {                                                       \
+    if (!(s)) return fail(LBM_ERR_ARG, "null solver handle"); \
+    LBM_CUDA(cudaSetDevice((s)->c.cfg.device));              \
+  } while (0)
+
+lbm_status lbm_init(lbm_solver *s, double seed_amp) {
+  LBM_HANDLE(s);
+  if (!std::isfinite(seed_amp)) return fail(LBM_ERR_ARG, "seed_amp must be finite");
+  s->c.odd_next = 1;
+  LBM_CUDA(dispatch_init(s->c, seed_amp, 0));
+  s->steps = 0;
+  return LBM_OK;
+}
+
+lbm_status lbm_init_random(lbm_solver *s, double rho_sigma, double u_noise, uint64_t seed) {
+  LBM_HANDLE(s);
+  if (!std::isfinite(rho_sigma) || !std::isfinite(u_noise)) return fail(LBM_ERR_ARG, "non-finite noise");
+  s->c.odd_next = 1;
+  LBM_CUDA(dispatch_init_random(s->c, rho_sigma, u_noise, seed, 0));
+  s->steps = 0;
+  return LBM_OK;
+}
+
+lbm_status lbm_step(lbm_solver *s, int32_t report, void *stream) {
+  LBM_HANDLE(s);
+  LBM_CUDA(dispatch_step(s->c, report != 0, (cudaStream_t)stream));
+  if (s->c.ev && s->c.ev_used < s->c.ev_cap) s->c.ev_used++;
+  s->c.odd_next ^= 1;
+  s->steps += 1;
+  if (report) s->reported = true;
+  return LBM_OK;
+}
+
+lbm_status lbm_run(lbm_solver *s, int32_t count, int32_t report_last, void *stream) {
+  LBM_HANDLE(s);
+  if (count < 0) return fail(LBM_ERR_ARG, "count must be >= 0");
+  for (int32_t k = 0; k < count; ++k) {
+    const bool rep = report_last && k == count - 1;
+    LBM_CUDA(dispatch_step(s->c, rep, (cudaStream_t)stream));
+    if (s->c.ev && s->c.ev_used < s->c.ev_cap) s->c.ev_used++;
+    s->c.odd_next ^= 1;
+    s->steps += 1;
+    if (rep) s->reported = true;
+  }
+  return LBM_OK;
+}
+
+lbm_status lbm_field_sums(lbm_solver *s, double out[8]) {
+  LBM_HANDLE(s);
+  if (!out) return fail(LBM_ERR_ARG, "null output");
+  LBM_CUDA(cudaDeviceSynchronize());
+  LBM_CUDA(cudaMemcpy(out, s->c.sums, lbmk::NSUM * sizeof(double), cudaMemcpyDeviceToHost));
+  return LBM_OK;
+}
+
+lbm_status lbm_monitors(lbm_solver *s, int32_t interval, double diameter, double out[7]) {
+  if (!out) return fail(LBM_ERR_ARG, "null output");
+  double t[8];
+  lbm_status st = lbm_field_sums(s, t);
+  if (st != LBM_OK) return st;
+  const double n = (double)s->c.n;
+  const double div = (double)std::max(interval, 1);
+  for (int k = 0; k < 5; ++k) out[k] = std::sqrt(t[k] / n) / div;
+  const double scale = 0.5 * s->c.cfg.u0 * s->c.cfg.u0 * diameter * s->c.cfg.nz;
+  out[LBM_MON_DRAG] = t[5] / scale;
+  out[LBM_MON_LIFT] = t[6] / scale;
+  for (int k = 0; k < 7; ++k)
+    if (!std::isfinite(out[k])) return fail(LBM_ERR_NONFINITE, "a monitor is not finite: the run diverged");
+  return LBM_OK;
+}
+
+lbm_status lbm_field(lbm_solver *s, int32_t id, float **ptr) {
+  if (!s || !ptr) return fail(LBM_ERR_ARG, "null argument");
+  if (id < 0 || id >= LBM_NUM_FIELDS) return fail(LBM_ERR_ARG, "field id out of range");
+  *ptr = s->c.fld[id];
+  return LBM_OK;
+}
+
+lbm_status lbm_set_field(lbm_solver *s, int32_t id, const float *host) {
+  LBM_HANDLE(s);
+  if (!host || id < 0 || id >= LBM_NUM_FIELDS) return fail(LBM_ERR_ARG, "bad field id or null buffer");
+  LBM_CUDA(cudaDeviceSynchronize());
+  LBM_CUDA(cudaMemcpy(s->c.fld[id], host, (size_t)s->c.n * sizeof(float), cudaMemcpyDefault));
+  return LBM_OK;
+}
+
+lbm_status lbm_set_physics(lbm_solver *s, int32_t collision, double nu, double cs) {
+  if (!s) return fail(LBM_ERR_ARG, "null solver handle");
+  lbm_config g = s->c.cfg;
+  g.collision = collision;
+  g.nu = nu;
+  if (cs >= 0) g.cs = cs;
+  lbm_status st = validate(g);
+  if (st != LBM_OK) return st;
+  s->c.cfg = g;
+  return LBM_OK;
+}
+
+lbm_status lbm_set_sponge(lbm_solver *s, double start, double strength) {
+  if (!s) return fail(LBM_ERR_ARG, "null solver handle");
+  if (!std::isfinite(start) || !std::isfinite(strength)) return fail(LBM_ERR_ARG, "non-finite sponge");
+  s->c.cfg.sponge_start = start;
+  s->c.cfg.sponge_strength = strength;
+  return LBM_OK;
+}
+
+lbm_status lbm_set_actuation(lbm_solver *s, double omega_rot) {
+  if (!s) return fail(LBM_ERR_ARG, "null solver handle");
+  if (!std::isfinite(omega_rot)) return fail(LBM_ERR_ARG, "non-finite rotation");
+  s->c.omega_rot = omega_rot;
+  return LBM_OK;
+}
+
+lbm_status lbm_get_actuation(lbm_solver *s, double *omega_rot) {
+  if (!s || !omega_rot) return fail(LBM_ERR_ARG, "null argument");
+  *omega_rot = s->c.omega_rot;
+  return LBM_OK;
+}
+
+static lbm_status copy_in(lbm_solver *s, const void *f, int32_t dtype, int32_t where) {
+  const size_t bytes = (size_t)19 * (size_t)s->c.n * (dtype == LBM_F64 ? 8 : 4);
+  if (where == LBM_DEVICE) {
+    LBM_CUDA(dispatch_import(s->c, f, dtype, 0));
+    LBM_CUDA(cudaDeviceSynchronize());
+    return LBM_OK;
+  }
+  void *tmp = nullptr;
+  LBM_CUDA(cudaMalloc(&tmp, bytes));
+  cudaError_t e = cudaMemcpy(tmp, f, bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = dispatch_import(s->c, tmp, dtype, 0);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  cudaFree(tmp);
+  if (e != cudaSuccess) return fail(LBM_ERR_CUDA, std::string("set_populations: ") + cudaGetErrorString(e));
+  return LBM_OK;
+}
+
+static lbm_status copy_out(lbm_solver *s, void *f, int32_t dtype, int32_t where) {
+  const size_t bytes = (size_t)19 * (size_t)s->c.n * (dtype == LBM_F64 ? 8 : 4);
+  if (where == LBM_DEVICE) {
+    LBM_CUDA(dispatch_export(s->c, f, dtype, 0));
+    LBM_CUDA(cudaDeviceSynchronize());
+    return LBM_OK;
+  }
+  void *tmp = nullptr;
+  LBM_CUDA(cudaMalloc(&tmp, bytes));
+  cudaError_t e = dispatch_export(s->c, tmp, dtype, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(f, tmp, bytes, cudaMemcpyDeviceToHost);
+  cudaFree(tmp);
+  if (e != cudaSuccess) return fail(LBM_ERR_CUDA, std::string("get_populations: ") + cudaGetErrorString(e));
+  return LBM_OK;
+}
+
+lbm_status lbm_set_populations(lbm_solver *s, const void *f, int32_t dtype, int32_t where) {
+  LBM_HANDLE(s);
+  if (!f || (dtype != LBM_F32 && dtype != LBM_F64) || (where != LBM_HOST && where != LBM_DEVICE))
+    return fail(LBM_ERR_ARG, "bad populations buffer, dtype or location");
+  LBM_CUDA(cudaDeviceSynchronize());
+  s->c.odd_next = 1;
+  s->steps = 0;
+  return copy_in(s, f, dtype, where);
+}
+
+lbm_status lbm_get_populations(lbm_solver *s, void *f, int32_t dtype, int32_t where) {
+  LBM_HANDLE(s);
+  if (!f || (dtype != LBM_F32 && dtype != LBM_F64) || (where != LBM_HOST && where != LBM_DEVICE))
+    return fail(LBM_ERR_ARG, "bad populations buffer, dtype or location");
+  LBM_CUDA(cudaDeviceSynchronize());
+  return copy_out(s, f, dtype, where);
+}
+
+lbm_status lbm_set_obstacle(lbm_solver *s, int32_t kind, const double geo[7]) {
+  LBM_HANDLE(s);
+  if (!geo) return fail(LBM_ERR_ARG, "null geometry");
+  lbm_config g = s->c.cfg;
+  g.obstacle = kind;
+  g.ox = geo[0];
+  g.oy = geo[1];
+  g.oz = geo[2];
+  g.r = geo[3];
+  g.hx = geo[4];
+  g.hy = geo[5];
+  g.hz = geo[6];
+  lbm_status st = validate(g);
+  if (st != LBM_OK) return st;
+  // carry the populations over: read them out with the old geometry, write them
+  // back (start-of-step layout) with the new one
+  const int dtype = g.storage == LBM_F64 ? LBM_F64 : LBM_F32;
+  const size_t bytes = (size_t)19 * (size_t)s->c.n * (dtype == LBM_F64 ? 8 : 4);
+  void *tmp = nullptr;
+  LBM_CUDA(cudaDeviceSynchronize());
+  LBM_CUDA(cudaMalloc(&tmp, bytes));
+  cudaError_t e = dispatch_export(s->c, tmp, dtype, 0);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    cudaFree(tmp);
+    return fail(LBM_ERR_CUDA, std::string("set_obstacle: ") + cudaGetErrorString(e));
+  }
+  s->c.cfg = g;
+  st = classify_blocks(s);
+  if (st == LBM_OK) {
+    s->c.odd_next = 1;
+    e = dispatch_import(s->c, tmp, dtype, 0);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) st = fail(LBM_ERR_CUDA, std::string("set_obstacle: ") + cudaGetErrorString(e));
+  }
+  cudaFree(tmp);
+  return st;
+}
+
+lbm_status lbm_set_output_stride(lbm_solver *s, int32_t stride) {
+  LBM_HANDLE(s);
+  if (stride < 1) return fail(LBM_ERR_ARG, "stride must be >= 1");
+  LBM_CUDA(cudaDeviceSynchronize());
+  Ctx &c = s->c;
+  release_output(c);
+  if (stride == 1) return LBM_OK;
+  const int dims[3] = {c.cfg.nx, c.cfg.ny, c.cfg.nz};
+  size_t m = 1;
+  for (int k = 0; k < 3; ++k) {
+    c.out_dims[k] = (dims[k] + stride - 1) / stride;
+    m *= (size_t)c.out_dims[k];
+  }
+  for (int k = 0; k < 5; ++k) {
+    c.out[k] = nullptr;
+    cudaError_t e = cudaMallocManaged(&c.out[k], m * sizeof(float), cudaMemAttachGlobal);
+    if (e != cudaSuccess) {
+      for (int j = 0; j < k; ++j) cudaFree(c.out[j]);
+      for (int j = 0; j < 5; ++j) c.out[j] = c.fld[j];
+      c.out_dims[0] = c.cfg.nx;
+      c.out_dims[1] = c.cfg.ny;
+      c.out_dims[2] = c.cfg.nz;
+      return fail(LBM_ERR_CUDA, std::string("output fields: ") + cudaGetErrorString(e));
+    }
+    cudaMemset(c.out[k], 0, m * sizeof(float));
+  }
+  LBM_CUDA(cudaDeviceSynchronize());
+  c.out_stride = stride;
+  return LBM_OK;
+}
+
+lbm_status lbm_output(lbm_solver *s, int32_t id, float **ptr, int64_t *count) {
+  if (!s || !ptr || !count) return fail(LBM_ERR_ARG, "null argument");
+  if (id < 0 || id >= 5) return fail(LBM_ERR_ARG, "output id out of range (ux, uy, uz, p, vmag)");
+  *ptr = s->c.out[id];
+  *count = (int64_t)s->c.out_dims[0] * s->c.out_dims[1] * s->c.out_dims[2];
+  return LBM_OK;
+}
+
+lbm_status lbm_update_output(lbm_solver *s, void *stream) {
+  LBM_HANDLE(s);
+  LBM_CUDA(lbmh::launch_coarsen(s->c, (cudaStream_t)stream));
+  return LBM_OK;
+}
+
+lbm_status lbm_mask(lbm_solver *s, uint8_t *host_out) {
+  LBM_HANDLE(s);
+  if (!host_out) return fail(LBM_ERR_ARG, "null output");
+  uint8_t *tmp = nullptr;
+  LBM_CUDA(cudaMalloc(&tmp, (size_t)s->c.n));
+  cudaError_t e = lbmh::launch_mask(s->c, tmp, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(host_out, tmp, (size_t)s->c.n, cudaMemcpyDeviceToHost);
+  cudaFree(tmp);
+  if (e != cudaSuccess) return fail(LBM_ERR_CUDA, std::string("mask: ") + cudaGetErrorString(e));
+  return LBM_OK;
+}
+
+lbm_status lbm_step_count(lbm_solver *s, int64_t *count) {
+  if (!s || !count) return fail(LBM_ERR_ARG, "null argument");
+  *count = s->steps;
+  return LBM_OK;
+}
+
+lbm_status lbm_memory(lbm_solver *s, int64_t *bytes) {
+  if (!s || !bytes) return fail(LBM_ERR_ARG, "null argument");
+  *bytes = s->bytes;
+  return LBM_OK;
+}
+
+lbm_status lbm_managed_alloc(int64_t count, float **ptr) {
+  if (!ptr || count < 1) return fail(LBM_ERR_ARG, "count must be >= 1 and ptr non-null");
+  *ptr = nullptr;
+  LBM_CUDA(cudaMallocManaged(ptr, (size_t)count * sizeof(float), cudaMemAttachGlobal));
+  LBM_CUDA(cudaMemset(*ptr, 0, (size_t)count * sizeof(float)));
+  LBM_CUDA(cudaDeviceSynchronize());
+  return LBM_OK;
+}
+
+lbm_status lbm_managed_free(float *ptr) {
+  if (ptr) LBM_CUDA(cudaFree(ptr));
+  return LBM_OK;
+}
+
+lbm_status lbm_timing(lbm_solver *s, int32_t enable) {
+  LBM_HANDLE(s);
+  LBM_CUDA(cudaDeviceSynchronize());
+  Ctx &c = s->c;
+  release_timing(c);
+  if (!enable) return LBM_OK;
+  const int cap = 4096;
+  c.ev = new (std::nothrow) cudaEvent_t[3 * cap];
+  if (!c.ev) return fail(LBM_ERR_ARG, "out of host memory");
+  for (int k = 0; k < 3 * cap; ++k) {
+    cudaError_t e = cudaEventCreate(&c.ev[k]);
+    if (e != cudaSuccess) {
+      for (int j = 0; j < k; ++j) cudaEventDestroy(c.ev[j]);
+      delete[] c.ev;
+      c.ev = nullptr;
+      return fail(LBM_ERR_CUDA, std::string("cudaEventCreate: ") + cudaGetErrorString(e));
+    }
+  }
+  c.ev_cap = cap;
+  c.ev_used = 0;
+  // cells owned by each kernel
+  std::vector<int> list(c.nspecial);
+  if (c.nspecial)
+    LBM_CUDA(cudaMemcpy(list.data(), c.special_list, list.size() * sizeof(int), cudaMemcpyDeviceToHost));
+  int64_t gen = 0;
+  for (int packed : list) {
+    const int bx = packed % c.gx, by = (packed / c.gx) % c.gy;
+    const int64_t wx = std::min(lbmk::BX, c.cfg.nx - bx * lbmk::BX);
+    const int64_t wy = std::min(lbmk::BY, c.cfg.ny - by * lbmk::BY);
+    gen += wx * wy;
+  }
+  c.generic_cells = gen;
+  c.bulk_cells = c.n - gen;
+  return LBM_OK;
+}
+
+lbm_status lbm_timing_read(lbm_solver *s, double out[7]) {
+  LBM_HANDLE(s);
+  if (!out) return fail(LBM_ERR_ARG, "null output");
+  LBM_CUDA(cudaDeviceSynchronize());
+  const Ctx &c = s->c;
+  double bulk = 0.0, gen = 0.0;
+  for (int k = 0; k < c.ev_used; ++k) {
+    float a = 0.f, b = 0.f;
+    LBM_CUDA(cudaEventElapsedTime(&a, c.ev[3 * k], c.ev[3 * k + 1]));
+    LBM_CUDA(cudaEventElapsedTime(&b, c.ev[3 * k + 1], c.ev[3 * k + 2]));
+    bulk += a;
+    gen += b;
+  }
+  float span = 0.f;
+  if (c.ev_used > 0) LBM_CUDA(cudaEventElapsedTime(&span, c.ev[0], c.ev[3 * (c.ev_used - 1) + 2]));
+  out[6] = span;
+  out[0] = bulk;
+  out[1] = c.ev_used;
+  out[2] = (double)c.bulk_cells;
+  out[3] = gen;
+  out[4] = c.nspecial > 0 ? c.ev_used : 0;
+  out[5] = (double)c.generic_cells;
+  return LBM_OK;
+}
+
+lbm_status lbm_sync(lbm_solver *s) {
+  LBM_HANDLE(s);
+  LBM_CUDA(cudaDeviceSynchronize());
+  return LBM_OK;
+}
+
+}  // extern "C"

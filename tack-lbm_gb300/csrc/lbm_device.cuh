@@ -1,0 +1,710 @@
+// lbm_device.cuh - device code of the D3Q19 AA-pattern stream-and-collide step.
+//
+// Layout in HBM: one structure-of-arrays buffer F with 19 slots of n cells,
+// F[q][idx], idx = (z*ny + y)*nx + x, x fastest (the reference layout,
+// lbm.py:397-402, lbm.py:426). The buffer is updated in place with the
+// AA pattern: an "odd" step reads the populations arriving at a cell from its
+// neighbours' slots and writes its post-collision populations into the slots
+// its neighbours will read locally; an "even" step reads and writes only the
+// cell's own slots (with directions swapped). Each cell touches the same
+// locations it reads, so the update needs no second buffer.
+//
+// Storage of a population is its deviation from the lattice weight,
+// delta_q = f_q - w_q, in FP16/BF16; FP32 and FP64 store f_q itself. All
+// arithmetic runs on deviations (float for FP32/16/BF16, double for FP64).
+//
+// Boundary handling follows the reference kernel (lbm.py:410-432):
+//   * halfway bounce-back from obstacle cells with the moving-wall term
+//     6 w_q c_q.u_w at the link midpoint, and the momentum-exchange force;
+//   * periodic x, periodic or free-slip (specular) y (PeriodicY/SlipY,
+//     lbm.py:342-369), and the z analogues; a moving no-slip lid above
+//     y = ny-1 for LBM_LID.
+// In the AA scheme a fluid cell's post-collision population that streams
+// into an obstacle cell is parked in that obstacle cell's slot, which no
+// other cell reads or writes; the fluid cell picks it up (bounced) on the
+// next step. Obstacle cells therefore never store anything: every reference
+// step resets them to w_q (sigma = 1, lbm.py:449-456) and nothing reads their
+// own values except their own bounce-back links, for which w_q is used.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include <type_traits>
+#include <utility>
+
+namespace lbmk {
+
+// f(std::integral_constant<int, 0>{}), ..., f(std::integral_constant<int, N-1>{}):
+// a loop whose index is a compile-time constant in the body.
+template <typename F, int... I>
+__host__ __device__ __forceinline__ void static_for_impl(F &&f, std::integer_sequence<int, I...>) {
+  (f(std::integral_constant<int, I>{}), ...);
+}
+template <int N, typename F>
+__host__ __device__ __forceinline__ void static_for(F &&f) {
+  static_for_impl(f, std::make_integer_sequence<int, N>{});
+}
+
+constexpr int Q = 19;
+constexpr int BX = 32;   // cells per warp along x
+constexpr int BY = 4;    // rows (warps) per block
+constexpr int NSUM = 8;  // r_rho, r_ux, r_uy, r_uz, r_ke, fx, fy, fz
+
+// D3Q19 ordering of the reference (lbm.py:15-17)
+__host__ __device__ constexpr int cx(int q) {
+  return q == 1 || q == 7 || q == 9 || q == 11 || q == 13 ? 1
+       : q == 2 || q == 8 || q == 10 || q == 12 || q == 14 ? -1 : 0;
+}
+__host__ __device__ constexpr int cy(int q) {
+  return q == 3 || q == 7 || q == 10 || q == 15 || q == 17 ? 1
+       : q == 4 || q == 8 || q == 9 || q == 16 || q == 18 ? -1 : 0;
+}
+__host__ __device__ constexpr int cz(int q) {
+  return q == 5 || q == 11 || q == 14 || q == 15 || q == 18 ? 1
+       : q == 6 || q == 12 || q == 13 || q == 16 || q == 17 ? -1 : 0;
+}
+// index of the direction (ex, ey, ez)
+__host__ __device__ constexpr int dir(int ex, int ey, int ez) {
+  int r = -1;
+  for (int q = 0; q < Q; ++q)
+    if (cx(q) == ex && cy(q) == ey && cz(q) == ez) r = q;
+  return r;
+}
+__host__ __device__ constexpr int opp(int q) { return dir(-cx(q), -cy(q), -cz(q)); }
+
+// lattice weights as the reference uploads them: float32 (lbm.py:18, lbm.py:48)
+__host__ __device__ constexpr float wq(int q) {
+  return q == 0 ? 1.0f / 3.0f : (q <= 6 ? 1.0f / 18.0f : 1.0f / 36.0f);
+}
+// sum of the float32 weights minus one (2^-26): rho = 1 + sum(delta) + W_EXCESS
+constexpr double W_EXCESS = 1.4901161193847656e-08;
+
+enum { COLL_BGK = 0, COLL_TRT = 1, COLL_LES = 2 };
+enum { OBS_NONE = 0, OBS_CYL = 1, OBS_SPH = 2, OBS_BOX = 3 };
+enum { SIDE_PERIODIC = 0, SIDE_SLIP = 1, SIDE_LID = 2 };
+
+struct Geo {
+  int kind;
+  float ox, oy, oz, r2, inv_r, hx, hy, hz;
+  float r;
+};
+
+// Everything a step launch needs, passed by value (__grid_constant__).
+template <typename S> struct Store;
+
+template <typename S>
+struct StepArgs {
+  using P = typename Store<S>::T;  // arithmetic precision of the step
+  S *slot[Q];             // slot[q] = F + q*n
+  int nx, ny, nz, nxy;
+  Geo geo;
+  int lateral, vertical;
+  P u_lid;
+  P u0, sponge_start, sponge_strength, inv_sponge_len;
+  P omega_rot;
+  P omega_bgk, tau0, smag_c, magic;   // smag_c = 25.456 cs^2 (lbm.py:93)
+  float *fld[13];
+  double *partials;       // NSUM doubles per block (report steps)
+  const uint8_t *special; // 1 for blocks handled by the generic kernel
+  const int *special_list;
+  int gx, gy;             // grid dimensions in blocks (x, y)
+};
+
+// Geometry of a configuration in the float32 form the kernels evaluate
+// (r^2 rounded like the reference's r*r).
+template <typename Cfg>
+inline Geo make_geo(const Cfg &g) {
+  Geo o{};
+  o.kind = g.obstacle;
+  o.ox = (float)g.ox;
+  o.oy = (float)g.oy;
+  o.oz = (float)g.oz;
+  o.r = (float)g.r;
+  o.r2 = (float)g.r * (float)g.r;
+  o.inv_r = g.r != 0.0 ? (float)(1.0 / g.r) : 0.0f;
+  o.hx = (float)g.hx;
+  o.hy = (float)g.hy;
+  o.hz = (float)g.hz;
+  return o;
+}
+
+// grid for the one-thread-per-cell utility kernels (grid-stride loops)
+inline int cell_grid(long long n) {
+  const long long b = (n + 255) / 256;
+  return (int)(b < 152 * 32 ? b : 152 * 32);
+}
+
+// ---------------------------------------------------------------------------
+// storage traits: load a deviation, store a deviation
+
+// load/store work on deviations d = f - w_q; load_value/store_value move the
+// population value f itself (host exchange), rounding once.
+template <> struct Store<float> {
+  using T = float;
+  template <int q> __device__ static float load(const float *p) { return *p - wq(q); }
+  template <int q> __device__ static void store(float *p, float d) { *p = d + wq(q); }
+  template <int q> __device__ static double load_value(const float *p) { return (double)*p; }
+  template <int q> __device__ static void store_value(float *p, double v) { *p = (float)v; }
+};
+template <> struct Store<double> {
+  using T = double;
+  template <int q> __device__ static double load(const double *p) { return *p - (double)wq(q); }
+  template <int q> __device__ static void store(double *p, double d) { *p = d + (double)wq(q); }
+  template <int q> __device__ static double load_value(const double *p) { return *p; }
+  template <int q> __device__ static void store_value(double *p, double v) { *p = v; }
+};
+template <> struct Store<__half> {
+  using T = float;
+  template <int q> __device__ static float load(const __half *p) { return __half2float(*p); }
+  template <int q> __device__ static void store(__half *p, float d) { *p = __float2half_rn(d); }
+  template <int q> __device__ static double load_value(const __half *p) {
+    return (double)wq(q) + (double)__half2float(*p);
+  }
+  template <int q> __device__ static void store_value(__half *p, double v) {
+    *p = __double2half(v - (double)wq(q));
+  }
+};
+template <> struct Store<__nv_bfloat16> {
+  using T = float;
+  template <int q> __device__ static float load(const __nv_bfloat16 *p) { return __bfloat162float(*p); }
+  template <int q> __device__ static void store(__nv_bfloat16 *p, float d) { *p = __float2bfloat16_rn(d); }
+  template <int q> __device__ static double load_value(const __nv_bfloat16 *p) {
+    return (double)wq(q) + (double)__bfloat162float(*p);
+  }
+  template <int q> __device__ static void store_value(__nv_bfloat16 *p, double v) {
+    *p = __double2bfloat16(v - (double)wq(q));
+  }
+};
+
+// ---------------------------------------------------------------------------
+// geometry: the reference's solid() tests evaluated in float32 with every
+// product and sum rounded separately (no fused multiply-add), so the mask is
+// reproducible on the host bit for bit (lbm.py:150-153, 177-182, 207-211).
+
+__device__ __forceinline__ bool solid(const Geo &g, int x, int y, int z) {
+  const float fx = (float)x, fy = (float)y, fz = (float)z;
+  if (g.kind == OBS_CYL) {
+    const float dx = __fsub_rn(fx, g.ox), dy = __fsub_rn(fy, g.oy);
+    return __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) < g.r2;
+  }
+  if (g.kind == OBS_SPH) {
+    const float dx = __fsub_rn(fx, g.ox), dy = __fsub_rn(fy, g.oy), dz = __fsub_rn(fz, g.oz);
+    return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)) < g.r2;
+  }
+  if (g.kind == OBS_BOX) {
+    const float ax = __fsub_rn(fabsf(__fsub_rn(fx, g.ox)), g.hx);
+    const float ay = __fsub_rn(fabsf(__fsub_rn(fy, g.oy)), g.hy);
+    const float az = __fsub_rn(fabsf(__fsub_rn(fz, g.oz)), g.hz);
+    return fmaxf(fmaxf(ax, ay), az) < 0.0f;
+  }
+  return false;
+}
+
+// ---------------------------------------------------------------------------
+// collision on deviations.
+//
+// With delta_q = f_q - w_q, rho = 1 + drho, and X_q = 3 c.u + 4.5 (c.u)^2 - 1.5 u^2,
+// the equilibrium deviation is feq_q - w_q = w_q (drho + rho X_q) (lbm.py:52-55).
+// For a direction q and its opposite, with s = c_q.u:
+//   A = drho - 1.5 rho u^2 + 4.5 rho s^2,  B = 3 rho s,
+//   feq_q - w_q = w_q (A + B),  feq_opp - w_opp = w_q (A - B).
+
+// the 9 direction pairs (q, opp q) with q odd-numbered in the reference order
+__host__ __device__ constexpr int pq(int k) { return 2 * k + 1; }
+
+template <typename T>
+struct Moments {
+  T drho, rho, ux, uy, uz;
+};
+
+template <typename T, int k>
+__device__ __forceinline__ T pair_dot(T ux, T uy, T uz) {
+  constexpr int q = pq(k);
+  T s = T(0);
+  if (cx(q) == 1) s += ux;
+  if (cx(q) == -1) s -= ux;
+  if (cy(q) == 1) s += uy;
+  if (cy(q) == -1) s -= uy;
+  if (cz(q) == 1) s += uz;
+  if (cz(q) == -1) s -= uz;
+  return s;
+}
+
+// equilibrium deviations of all 19 directions
+template <typename T>
+__device__ __forceinline__ void feq_dev(T drho, T rho, T ux, T uy, T uz, T eq[Q]) {
+  const T base = drho - T(1.5) * rho * (ux * ux + uy * uy + uz * uz);
+  const T r45 = T(4.5) * rho, r3 = T(3.0) * rho;
+  eq[0] = T(wq(0)) * base;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    const int q = pq(k);
+    T s;
+    switch (k) {
+      case 0: s = pair_dot<T, 0>(ux, uy, uz); break;
+      case 1: s = pair_dot<T, 1>(ux, uy, uz); break;
+      case 2: s = pair_dot<T, 2>(ux, uy, uz); break;
+      case 3: s = pair_dot<T, 3>(ux, uy, uz); break;
+      case 4: s = pair_dot<T, 4>(ux, uy, uz); break;
+      case 5: s = pair_dot<T, 5>(ux, uy, uz); break;
+      case 6: s = pair_dot<T, 6>(ux, uy, uz); break;
+      case 7: s = pair_dot<T, 7>(ux, uy, uz); break;
+      default: s = pair_dot<T, 8>(ux, uy, uz); break;
+    }
+    const T A = r45 * s * s + base;
+    const T B = r3 * s;
+    const T w = T(wq(q));
+    eq[q] = w * (A + B);
+    eq[q + 1] = w * (A - B);
+  }
+}
+
+template <typename T> __device__ __forceinline__ T fsqrt(T v);
+template <> __device__ __forceinline__ float fsqrt<float>(float v) { return __fsqrt_rn(v); }
+template <> __device__ __forceinline__ double fsqrt<double>(double v) { return sqrt(v); }
+
+// Relax the deviations d[] in place. Returns nothing; moments in m.
+// BGK (lbm.py:60-69), TRT + Smagorinsky (lbm.py:96-123), LES-BGK (lbm.py:126-139).
+template <typename T, int COLL>
+__device__ __forceinline__ void collide(T d[Q], const Moments<T> &m, T omega_bgk, T tau0,
+                                        T smag_c, T magic) {
+  T eq[Q];
+  feq_dev<T>(m.drho, m.rho, m.ux, m.uy, m.uz, eq);
+  if (COLL == COLL_BGK) {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) d[q] = d[q] - omega_bgk * (d[q] - eq[q]);
+    return;
+  }
+  // Smagorinsky relaxation time from the non-equilibrium stress (lbm.py:72-93)
+  T neq[Q];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) neq[q] = d[q] - eq[q];
+  T pxx = T(0), pyy = T(0), pzz = T(0), pxy = T(0), pxz = T(0), pyz = T(0);
+#pragma unroll
+  for (int q = 1; q < Q; ++q) {
+    if (cx(q) != 0) pxx += neq[q];
+    if (cy(q) != 0) pyy += neq[q];
+    if (cz(q) != 0) pzz += neq[q];
+    if (cx(q) * cy(q) == 1) pxy += neq[q];
+    if (cx(q) * cy(q) == -1) pxy -= neq[q];
+    if (cx(q) * cz(q) == 1) pxz += neq[q];
+    if (cx(q) * cz(q) == -1) pxz -= neq[q];
+    if (cy(q) * cz(q) == 1) pyz += neq[q];
+    if (cy(q) * cz(q) == -1) pyz -= neq[q];
+  }
+  const T pi = fsqrt<T>(pxx * pxx + pyy * pyy + pzz * pzz + T(2) * (pxy * pxy + pxz * pxz + pyz * pyz));
+  const T tau = T(0.5) * (tau0 + fsqrt<T>(tau0 * tau0 + smag_c * pi / m.rho));
+  if (COLL == COLL_LES) {
+    const T om = T(1) / tau;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) d[q] = d[q] - om * neq[q];
+    return;
+  }
+  // TRT: even/odd parts relaxed at omega+ = 1/tau, omega- = 1/(magic/(tau-1/2)+1/2)
+  const T hp = T(0.5) / tau;
+  const T hm = T(0.5) / (magic / (tau - T(0.5)) + T(0.5));
+  d[0] = d[0] - T(2) * hp * neq[0];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    const int q = pq(k);
+    const T sym = hp * (neq[q] + neq[q + 1]);
+    const T anti = hm * (neq[q] - neq[q + 1]);
+    d[q] = d[q] - sym - anti;
+    d[q + 1] = d[q + 1] - sym + anti;
+  }
+}
+
+// moments of the deviations; fluid = 0 gives u = 0 (lbm.py:433-444)
+template <typename T>
+__device__ __forceinline__ Moments<T> moments(const T d[Q], bool fluid) {
+  T s = T(0), jx = T(0), jy = T(0), jz = T(0);
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    s += d[q];
+    if (cx(q) == 1) jx += d[q];
+    if (cx(q) == -1) jx -= d[q];
+    if (cy(q) == 1) jy += d[q];
+    if (cy(q) == -1) jy -= d[q];
+    if (cz(q) == 1) jz += d[q];
+    if (cz(q) == -1) jz -= d[q];
+  }
+  Moments<T> m;
+  m.drho = s + T(W_EXCESS);
+  m.rho = T(1) + m.drho;
+  const T inv = fluid ? T(1) / m.rho : T(0);
+  m.ux = jx * inv;
+  m.uy = jy * inv;
+  m.uz = jz * inv;
+  return m;
+}
+
+// Sponge blend toward (1, u0*fluid, 0, 0) (lbm.py:446-456):
+// out = feq(rho_s, u_s) + (1 - sigma)(post - feq(rho, u)), in deviations.
+template <typename T>
+__device__ __forceinline__ void sponge(T d[Q], const Moments<T> &m, T sigma, T u0fluid) {
+  T e0[Q], e1[Q];
+  feq_dev<T>(m.drho, m.rho, m.ux, m.uy, m.uz, e0);
+  const T drho_s = m.drho - sigma * m.drho;
+  const T rho_s = T(1) + drho_s;
+  const T ux_s = m.ux + sigma * (u0fluid - m.ux);
+  const T uy_s = (T(1) - sigma) * m.uy;
+  const T uz_s = (T(1) - sigma) * m.uz;
+  feq_dev<T>(drho_s, rho_s, ux_s, uy_s, uz_s, e1);
+  const T keep = T(1) - sigma;
+#pragma unroll
+  for (int q = 0; q < Q; ++q) d[q] = e1[q] + keep * (d[q] - e0[q]);
+}
+
+// ---------------------------------------------------------------------------
+// report-step reduction: 8 per-cell values summed in FP64 per block
+
+__device__ __forceinline__ void block_sums(const float v[NSUM], double *partials, int bid) {
+  __shared__ double red[BY][NSUM];
+  const int lane = threadIdx.x, warp = threadIdx.y;
+#pragma unroll
+  for (int k = 0; k < NSUM; ++k) {
+    double s = (double)v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) red[warp][k] = s;
+  }
+  __syncthreads();
+  if (warp == 0 && lane < NSUM) {
+    double s = 0.0;
+#pragma unroll
+    for (int w = 0; w < BY; ++w) s += red[w][lane];
+    partials[(size_t)bid * NSUM + lane] = s;
+  }
+}
+
+// Diagnostics of one cell (lbm.py:493-513); v[] receives the values summed by monitors().
+template <typename T>
+__device__ __forceinline__ void diagnostics(float *const fld[13], int idx, const Moments<T> &m,
+                                            float mx, float my, float mz, float v[NSUM]) {
+  const float rho = (float)m.rho;
+  const float ux = (float)m.ux, uy = (float)m.uy, uz = (float)m.uz;
+  const float p = (float)(m.drho / T(3));
+  const float ke = 0.5f * rho * (ux * ux + uy * uy + uz * uz);
+  const float ox = fld[0][idx], oy = fld[1][idx], oz = fld[2][idx], op = fld[3][idx];
+  const float ok = 0.5f * (ox * ox + oy * oy + oz * oz);
+  const float dp = 3.0f * (p - op);
+  v[0] = dp * dp;
+  v[1] = (ux - ox) * (ux - ox);
+  v[2] = (uy - oy) * (uy - oy);
+  v[3] = (uz - oz) * (uz - oz);
+  v[4] = (ke - ok) * (ke - ok);
+  v[5] = mx;
+  v[6] = my;
+  v[7] = mz;
+  fld[0][idx] = ux;
+  fld[1][idx] = uy;
+  fld[2][idx] = uz;
+  fld[3][idx] = p;
+  fld[4][idx] = sqrtf(ux * ux + uy * uy + uz * uz);
+#pragma unroll
+  for (int k = 0; k < 5; ++k) fld[5 + k][idx] = v[k];
+  fld[10][idx] = mx;
+  fld[11][idx] = my;
+  fld[12][idx] = mz;
+}
+
+__device__ __forceinline__ int block_id() {
+  return ((int)blockIdx.z * (int)gridDim.y + (int)blockIdx.y) * (int)gridDim.x + (int)blockIdx.x;
+}
+
+// ---------------------------------------------------------------------------
+// Bulk kernel: blocks with no obstacle cell within reach and no wall row.
+// Every cell is fluid; x, y, z wrap periodically through per-lane / per-row
+// offsets. ODD selects the neighbour-reading half of the AA pair.
+
+template <typename S, int COLL, bool REPORT, bool ODD>
+__global__ void __launch_bounds__(BX * BY)
+bulk_kernel(const __grid_constant__ StepArgs<S> a) {
+  using T = typename Store<S>::T;
+  const int bid = block_id();
+  if (a.special[bid]) return;  // uniform per block
+  const int x = (int)blockIdx.x * BX + (int)threadIdx.x;
+  const int y = (int)blockIdx.y * BY + (int)threadIdx.y;
+  const int z = (int)blockIdx.z;
+  const bool active = x < a.nx && y < a.ny;
+  float v[NSUM] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (active) {
+    const int idx = (z * a.ny + y) * a.nx + x;
+    T d[Q];
+    int dxm = 0, dxp = 0, dym = 0, dyp = 0, dzm = 0, dzp = 0;
+    if (ODD) {
+      dxm = x == 0 ? a.nx - 1 : -1;
+      dxp = x == a.nx - 1 ? 1 - a.nx : 1;
+      dym = y == 0 ? (a.ny - 1) * a.nx : -a.nx;
+      dyp = y == a.ny - 1 ? -(a.ny - 1) * a.nx : a.nx;
+      dzm = z == 0 ? (a.nz - 1) * a.nxy : -a.nxy;
+      dzp = z == a.nz - 1 ? -(a.nz - 1) * a.nxy : a.nxy;
+    }
+    // offset of the cell x - c_q (the source of population q)
+    auto src_off = [&](auto qc) {
+      constexpr int q = decltype(qc)::value;
+      return (cx(q) == 1 ? dxm : cx(q) == -1 ? dxp : 0) + (cy(q) == 1 ? dym : cy(q) == -1 ? dyp : 0) +
+             (cz(q) == 1 ? dzm : cz(q) == -1 ? dzp : 0);
+    };
+    static_for<Q>([&](auto qc) {
+      constexpr int q = decltype(qc)::value;
+      if (ODD) d[q] = Store<S>::template load<q>(a.slot[opp(q)] + (idx + src_off(qc)));
+      else d[q] = Store<S>::template load<q>(a.slot[q] + idx);
+    });
+    const Moments<T> m = moments<T>(d, true);
+    collide<T, COLL>(d, m, a.omega_bgk, a.tau0, a.smag_c, a.magic);
+    const T t = fmax(T(0), (T(x) - a.sponge_start) * a.inv_sponge_len);
+    const T sigma = a.sponge_strength * t * t;
+    if (__any_sync(__activemask(), sigma != T(0))) sponge<T>(d, m, sigma, a.u0);
+    static_for<Q>([&](auto pc) {
+      constexpr int p = decltype(pc)::value;
+      // population p moves to x + c_p, the source cell of direction opp(p) seen from x
+      if (ODD) Store<S>::template store<p>(a.slot[p] + (idx + src_off(std::integral_constant<int, opp(p)>{})), d[p]);
+      else Store<S>::template store<p>(a.slot[opp(p)] + idx, d[p]);
+    });
+    if (REPORT) diagnostics<T>(a.fld, idx, m, 0.f, 0.f, 0.f, v);
+  }
+  if (REPORT) block_sums(v, a.partials, bid);
+}
+
+// ---------------------------------------------------------------------------
+// Generic kernel: the links of a cell evaluated one by one (lbm.py:410-432).
+
+template <typename S>
+struct Link {
+  S *L;        // where population q of this cell is read from on an odd step
+  bool lid;    // the link crosses the moving lid
+  bool wall;   // the source cell is an obstacle cell
+  typename Store<S>::T cu;  // c_q . u_wall (bounce links only)
+};
+
+template <typename S, int q>
+__device__ __forceinline__ Link<S> make_link(const StepArgs<S> &a, int x, int y, int z) {
+  using T = typename Store<S>::T;
+  Link<S> k;
+  int xs = x - cx(q);
+  xs += xs < 0 ? a.nx : 0;
+  xs -= xs >= a.nx ? a.nx : 0;
+  int ys = y - cy(q), zs = z - cz(q);
+  bool ry = false, rz = false;  // the source population is mirrored in y / z
+  k.lid = false;
+  if (a.lateral == SIDE_PERIODIC) {
+    ys += ys < 0 ? a.ny : 0;
+    ys -= ys >= a.ny ? a.ny : 0;
+  } else {
+    const bool lo = ys < 0, hi = ys >= a.ny;
+    k.lid = hi && a.lateral == SIDE_LID;
+    ry = lo || (hi && a.lateral == SIDE_SLIP);
+    ys = (ry || k.lid) ? y : ys;
+  }
+  if (a.vertical == SIDE_PERIODIC) {
+    zs += zs < 0 ? a.nz : 0;
+    zs -= zs >= a.nz ? a.nz : 0;
+  } else {
+    rz = zs < 0 || zs >= a.nz;
+    zs = rz ? z : zs;
+  }
+  k.wall = !k.lid && solid(a.geo, xs, ys, zs);
+  // the source population (cx, +-cy, +-cz) sits, in the even view, in the slot of its opposite
+  constexpr int s00 = opp(q);
+  constexpr int s01 = opp(dir(cx(q), cy(q), -cz(q)));
+  constexpr int s10 = opp(dir(cx(q), -cy(q), cz(q)));
+  constexpr int s11 = opp(dir(cx(q), -cy(q), -cz(q)));
+  S *base = ry ? (rz ? a.slot[s11] : a.slot[s10]) : (rz ? a.slot[s01] : a.slot[s00]);
+  k.L = base + ((zs * a.ny + ys) * a.nx + xs);
+  // moving-wall term at the link midpoint (lbm.py:417-425)
+  T cu = T(0);
+  if (k.lid) {
+    cu = T(cx(q)) * a.u_lid;
+  } else if (a.geo.kind == OBS_CYL) {
+    const T xm = T(x) - T(0.5) * T(cx(q));
+    const T ym = T(y) - T(0.5) * T(cy(q));
+    const T vx = a.omega_rot * (-(ym - T(a.geo.oy)) * T(a.geo.inv_r));
+    const T vy = a.omega_rot * ((xm - T(a.geo.ox)) * T(a.geo.inv_r));
+    cu = T(cx(q)) * vx + T(cy(q)) * vy;
+  }
+  k.cu = cu;
+  return k;
+}
+
+template <typename S>
+__device__ __forceinline__ void decode_special(const StepArgs<S> &a, int &bx, int &by, int &z) {
+  const int packed = a.special_list[blockIdx.x];
+  bx = packed % a.gx;
+  by = (packed / a.gx) % a.gy;
+  z = packed / (a.gx * a.gy);
+}
+
+template <typename S, int COLL, bool REPORT, bool ODD>
+__global__ void __launch_bounds__(BX * BY)
+generic_kernel(const __grid_constant__ StepArgs<S> a) {
+  using T = typename Store<S>::T;
+  int bx, by, z;
+  decode_special(a, bx, by, z);
+  const int x = bx * BX + (int)threadIdx.x;
+  const int y = by * BY + (int)threadIdx.y;
+  const bool active = x < a.nx && y < a.ny;
+  float v[NSUM] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const bool here = active && solid(a.geo, x, y, z);
+  if (active && (REPORT || !here)) {
+    const int idx = (z * a.ny + y) * a.nx + x;
+    T d[Q];
+    float mx = 0.f, my = 0.f, mz = 0.f;
+    static_for<Q>([&](auto qc) {
+      constexpr int q = decltype(qc)::value;
+      const Link<S> k = make_link<S, q>(a, x, y, z);
+      const bool bb = k.lid || k.wall;
+      const T wall_term = T(6) * T(wq(q)) * k.cu;
+      T val;
+      if (here) {
+        // obstacle cell: streamed-in values, or its own w_q (deviation 0) on its bounce links
+        if (bb) val = wall_term;
+        else val = ODD ? Store<S>::template load<q>(k.L) : Store<S>::template load<q>(a.slot[q] + idx);
+      } else {
+        S *src;
+        if (ODD) src = bb ? a.slot[q] + idx : k.L;
+        else src = k.wall ? k.L : a.slot[q] + idx;
+        const T got = Store<S>::template load<q>(src);
+        val = bb ? got + wall_term : got;
+        if (k.wall) {
+          // momentum exchange (lbm.py:429-432); bounced = w_q + the deviation just read
+          const float hit = (float)(T(2) * (got + T(wq(q))) + wall_term);
+          mx += hit * (float)(-cx(q));
+          my += hit * (float)(-cy(q));
+          mz += hit * (float)(-cz(q));
+        }
+      }
+      d[q] = val;
+    });
+    const Moments<T> m = moments<T>(d, !here);
+    if (!here) {
+      collide<T, COLL>(d, m, a.omega_bgk, a.tau0, a.smag_c, a.magic);
+      const T t = fmax(T(0), (T(x) - a.sponge_start) * a.inv_sponge_len);
+      const T sigma = a.sponge_strength * t * t;
+      if (sigma != T(0)) sponge<T>(d, m, sigma, a.u0);
+      static_for<Q>([&](auto pc) {
+        constexpr int p = decltype(pc)::value;
+        constexpr int o = opp(p);
+        S *dst;
+        if (ODD) {
+          const Link<S> k = make_link<S, o>(a, x, y, z);
+          dst = k.lid ? a.slot[o] + idx : k.L;
+        } else {
+          dst = a.slot[o] + idx;
+        }
+        Store<S>::template store<p>(dst, d[p]);
+      });
+    }
+    if (REPORT) diagnostics<T>(a.fld, idx, m, mx, my, mz, v);
+  }
+  if (REPORT) block_sums(v, a.partials, (z * a.gy + by) * a.gx + bx);
+}
+
+// ---------------------------------------------------------------------------
+// Population exchange in the reference layout f[q*n + idx] and initial states.
+
+__device__ __forceinline__ void decode(int idx, int nx, int ny, int &x, int &y, int &z) {
+  x = idx % nx;
+  y = (idx / nx) % ny;
+  z = idx / (nx * ny);
+}
+
+template <typename S, typename V>
+__global__ void import_kernel(const __grid_constant__ StepArgs<S> a, const V *src, int n) {
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    // even view: population q of cell idx sits in slot opp(q)
+    static_for<Q>([&](auto qc) {
+      constexpr int q = decltype(qc)::value;
+      Store<S>::template store_value<q>(a.slot[opp(q)] + idx, (double)src[(size_t)q * n + idx]);
+    });
+  }
+}
+
+// odd_next = 1: even view (slot opp(q) of the cell); 0: odd view (where the
+// last odd step put population q). Obstacle cells read back as w_q.
+template <typename S, typename V>
+__global__ void export_kernel(const __grid_constant__ StepArgs<S> a, V *dst, int n, int odd_next) {
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    int x, y, z;
+    decode(idx, a.nx, a.ny, x, y, z);
+    const bool here = solid(a.geo, x, y, z);
+    static_for<Q>([&](auto qc) {
+      constexpr int q = decltype(qc)::value;
+      constexpr int o = opp(q);
+      double v;
+      if (here) {
+        v = (double)wq(q);
+      } else if (odd_next) {
+        v = Store<S>::template load_value<q>(a.slot[o] + idx);
+      } else {
+        const Link<S> k = make_link<S, o>(a, x, y, z);
+        v = Store<S>::template load_value<q>(k.lid ? a.slot[o] + idx : k.L);
+      }
+      dst[(size_t)q * n + idx] = (V)v;
+    });
+  }
+}
+
+// lbm_init (lbm.py:383-394), written in the even view
+template <typename S>
+__global__ void init_kernel(const __grid_constant__ StepArgs<S> a, float seed_amp, int n) {
+  using T = typename Store<S>::T;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    int x, y, z;
+    decode(idx, a.nx, a.ny, x, y, z);
+    const T fluid = solid(a.geo, x, y, z) ? T(0) : T(1);
+    const T ux = a.u0 * fluid;
+    const float ang_x = 6.2831853f * (float)x / (float)a.nx;
+    const float ang_z = 6.2831853f * (float)z / (float)a.nz;
+    const T uy = T(seed_amp) * a.u0 * fluid * T(sinf(ang_x)) * T(cosf(ang_z));
+    T eq[Q];
+    feq_dev<T>(T(0), T(1), ux, uy, T(0), eq);
+    static_for<Q>([&](auto qc) {
+      constexpr int q = decltype(qc)::value;
+      Store<S>::template store<q>(a.slot[opp(q)] + idx, eq[q]);
+    });
+  }
+}
+
+// splitmix64 (Steele, Lea, Flood 2014; constants as published by Vigna)
+__host__ __device__ __forceinline__ uint64_t splitmix64(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+// uniform in (0, 1) from draw k of cell idx: 24 random bits, centred
+__host__ __device__ __forceinline__ float uniform01(uint64_t key, uint64_t idx, int k) {
+  const uint64_t h = splitmix64(key + idx * 8ull + (uint64_t)k);
+  return ((float)(uint32_t)(h >> 40) + 0.5f) * 5.9604644775390625e-08f;  // 2^-24
+}
+
+// Equilibrium with rho = 1 + rho_sigma N(0,1) and u = (u0,0,0) + U(-a,a)^3 in fluid cells.
+template <typename S>
+__global__ void init_random_kernel(const __grid_constant__ StepArgs<S> a, float rho_sigma,
+                                   float u_noise, uint64_t key, int n) {
+  using T = typename Store<S>::T;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    int x, y, z;
+    decode(idx, a.nx, a.ny, x, y, z);
+    T drho = T(0), ux = T(0), uy = T(0), uz = T(0);
+    if (!solid(a.geo, x, y, z)) {
+      const float u1 = uniform01(key, (uint64_t)idx, 0), u2 = uniform01(key, (uint64_t)idx, 1);
+      const float g = sqrtf(-2.0f * logf(u1)) * cosf(6.28318530717958647692f * u2);
+      drho = T(rho_sigma * g);
+      ux = a.u0 + T(u_noise * (2.0f * uniform01(key, (uint64_t)idx, 2) - 1.0f));
+      uy = T(u_noise * (2.0f * uniform01(key, (uint64_t)idx, 3) - 1.0f));
+      uz = T(u_noise * (2.0f * uniform01(key, (uint64_t)idx, 4) - 1.0f));
+    }
+    T eq[Q];
+    feq_dev<T>(drho, T(1) + drho, ux, uy, uz, eq);
+    static_for<Q>([&](auto qc) {
+      constexpr int q = decltype(qc)::value;
+      Store<S>::template store<q>(a.slot[opp(q)] + idx, eq[q]);
+    });
+  }
+}
+
+}  // namespace lbmk

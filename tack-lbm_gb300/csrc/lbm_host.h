@@ -1,0 +1,51 @@
+// lbm_host.h - host-side state shared by the C ABI and the per-precision kernel units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/lbm_gb300.h"
+
+namespace lbmh {
+
+// Everything the launch helpers need about one solver.
+struct Ctx {
+  lbm_config cfg;
+  int64_t n;                 // cells
+  void *F;                   // 19*n populations, storage precision cfg.storage
+  float *fld[LBM_NUM_FIELDS];
+  double *partials;          // 8 doubles per block (report steps)
+  double *stage;             // finalize stage: 8 doubles per finalize block
+  double *sums;              // 8 doubles: the last report step's FP64 sums
+  uint8_t *special;          // per block: 1 when the generic kernel owns it
+  int *special_list;         // packed block ids ((z*gy + by)*gx + bx)
+  int nspecial;
+  int gx, gy;                // blocks along x and y (32 x 4 cells each)
+  int64_t nblocks;           // gx*gy*nz
+  int odd_next;              // 1: the next step reads neighbours (state in "even view")
+  double omega_rot;
+  int out_stride;            // output grid subsampling (1: aliases fld)
+  int out_dims[3];
+  float *out[5];             // coarse ux, uy, uz, p, vmag (owned when out_stride > 1)
+  // optional kernel timing: events around the bulk and generic launches
+  cudaEvent_t *ev;           // 3 events per step in a ring (bulk start, bulk end/generic start, generic end)
+  int ev_cap, ev_used;
+  int64_t bulk_cells, generic_cells;
+};
+
+constexpr int FINALIZE_BLOCKS = 128;
+
+// per-precision entry points (explicitly instantiated in lbm_kernels_<p>.cu)
+template <typename S> cudaError_t launch_step(const Ctx &c, bool report, cudaStream_t st);
+template <typename S> cudaError_t launch_init(const Ctx &c, double seed_amp, cudaStream_t st);
+template <typename S> cudaError_t launch_init_random(const Ctx &c, double rho_sigma, double u_noise,
+                                                     uint64_t seed, cudaStream_t st);
+// src/dst: device pointers to 19*n values of float (dtype LBM_F32) or double (LBM_F64)
+template <typename S> cudaError_t launch_import(const Ctx &c, const void *src, int dtype, cudaStream_t st);
+template <typename S> cudaError_t launch_export(const Ctx &c, void *dst, int dtype, cudaStream_t st);
+
+cudaError_t launch_finalize(const Ctx &c, cudaStream_t st);
+cudaError_t launch_mask(const Ctx &c, uint8_t *dst_dev, cudaStream_t st);
+cudaError_t launch_coarsen(const Ctx &c, cudaStream_t st);
+
+}  // namespace lbmh

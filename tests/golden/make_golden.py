@@ -1,0 +1,206 @@
+"""Generate the golden vectors under tests/golden/ from the reference itself.
+
+Run in a container where the tack-lbm sources are mounted (default
+``/root/reference``, or pass the directory as the first argument):
+
+    python tests/golden/make_golden.py [REFERENCE_DIR]
+
+The reference's kernels are Tack programs; ``tack_shim`` lets them execute
+as plain Python loops in float64 (the populations and fields the reference
+stores as float32 are given float32 values on input). The script writes:
+
+* ``trt_ref.npz``   - ``trt_ref.py`` executed verbatim: its input, its NumPy TRT
+                      step (``ref``) and the reference kernel's result (``got``).
+* ``step_cases.npz``- one ``lbm_step`` per case over collision x obstacle x
+                      lateral policy x report, from seeded near-equilibrium states.
+* ``init_cases.npz``- ``lbm_init`` for each obstacle.
+* ``solver_cases.npz`` - whole ``Solver`` runs: construction (init plus the
+                      priming report step), quiet and report steps, a rotation
+                      change and ``monitors()``.
+
+Nothing reads the reference at test time; only these files are used.
+"""
+
+import json
+import os
+import runpy
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import tack_shim  # noqa: E402
+
+NX, NY, NZ = 12, 10, 6
+
+GEOMETRY = {
+    "cylinder": dict(ox=5.3, oy=4.7, oz=0.0, r=2.6),
+    "sphere": dict(ox=5.5, oy=4.5, oz=2.5, r=2.4),
+    "box": dict(ox=5.5, oy=5.0, oz=3.0, hx=1.5, hy=2.0, hz=1.2),
+}
+
+# (name, collision, obstacle, lateral, report, omega_rot)
+STEP_CASES = [
+    ("bgk_cylinder_periodic_report", "bgk", "cylinder", "periodic", True, 0.05),
+    ("trt_cylinder_slip_report", "trt", "cylinder", "slip", True, -0.03),
+    ("les_cylinder_slip_quiet", "les", "cylinder", "slip", False, 0.04),
+    ("les_sphere_slip_report", "les", "sphere", "slip", True, 0.0),
+    ("trt_sphere_periodic_quiet", "trt", "sphere", "periodic", False, 0.0),
+    ("les_box_periodic_report", "les", "box", "periodic", True, 0.0),
+    ("bgk_box_slip_quiet", "bgk", "box", "slip", False, 0.0),
+]
+
+SOLVER_CASES = [
+    dict(name="les_cylinder_slip", nx=24, ny=16, nz=8, collision="les", obstacle="cylinder",
+         reynolds=120.0, u0=0.07, diameter=6.0, lateral="slip", rotation=0.02),
+    dict(name="trt_sphere_periodic", nx=24, ny=16, nz=8, collision="trt", obstacle="sphere",
+         reynolds=300.0, u0=0.08, diameter=6.0, lateral="periodic", rotation=0.0),
+    dict(name="bgk_box_periodic", nx=20, ny=14, nz=10, collision="bgk", obstacle="box",
+         reynolds=80.0, u0=0.05, diameter=5.0, lateral="periodic", rotation=0.0),
+]
+
+
+def geometry(lbm, kind):
+    g = GEOMETRY[kind]
+    if kind == "cylinder":
+        return lbm.Cylinder(g["ox"], g["oy"], g["r"])
+    if kind == "sphere":
+        return lbm.Sphere(g["ox"], g["oy"], g["oz"], g["r"])
+    return lbm.Box(g["ox"], g["oy"], g["oz"], g["hx"], g["hy"], g["hz"])
+
+
+def seeded_state(lbm, geo, n, rng):
+    """Near-equilibrium float32 populations; solid cells at rest (f = w), as
+    every reference step leaves them (lbm.py:449-456 with sigma = 1)."""
+    c = np.array([lbm.CX, lbm.CY, lbm.CZ]).T
+    w = np.array(lbm.W, np.float32).astype(np.float64)
+    rho = 1 + 0.01 * rng.standard_normal(n)
+    u = np.array([0.06, 0.0, 0.0]) + 0.02 * rng.standard_normal((n, 3))
+    cu = 3.0 * (u @ c.T)
+    f = w * rho[:, None] * (1 + cu + 0.5 * cu ** 2 - 1.5 * (u ** 2).sum(1)[:, None])
+    f += 1e-3 * rng.standard_normal((n, 19))
+    idx = np.arange(n)
+    x, y, z = idx % NX, (idx // NX) % NY, idx // (NX * NY)
+    solid = np.array([geo.solid(int(a), int(b), int(d)) for a, b, d in zip(x, y, z)])
+    f[solid > 0] = w
+    return np.ascontiguousarray(f.T.reshape(-1)).astype(np.float32), solid
+
+
+def heat_stub(lbm, n):
+    h = lbm.Solver.__new__(lbm.Solver)
+    h.heat_enabled = False
+    h.nx = NX
+    h._setup_heat(n)
+    return h
+
+
+def make_trt_ref(ref_dir):
+    lbm = tack_shim.import_reference(ref_dir)
+    g = runpy.run_path(os.path.join(ref_dir, "trt_ref.py"), run_name="trt_ref")
+    assert lbm is sys.modules["lbm"]
+    err = float(np.abs(g["got"] - g["ref"]).max())
+    print(f"trt_ref: max |kernel - numpy| = {err:.3e}")
+    np.savez_compressed(os.path.join(HERE, "trt_ref.npz"),
+                        f_in=g["f_in"], ref=g["ref"].T.reshape(-1), got=g["got"].T.reshape(-1),
+                        dims=np.array([g["nx"], g["ny"], g["nz"]]), nu=np.array(0.002))
+
+
+def make_step_cases(ref_dir):
+    lbm = tack_shim.import_reference(ref_dir)
+    n = NX * NY * NZ
+    out, meta = {}, {}
+    for k, (name, coll, obst, lateral, report, omega_rot) in enumerate(STEP_CASES):
+        rng = np.random.default_rng(100 + k)
+        lat = lbm.D3Q19(NX, NY, NZ)
+        nu = 0.004 + 0.002 * k
+        phys = lbm.COLLISIONS[coll](nu)
+        geo = geometry(lbm, obst)
+        omega = tack_shim.HostManagedArray(1)
+        omega.numpy[0] = omega_rot
+        side = {"periodic": lbm.PeriodicY, "slip": lbm.SlipY}[lateral]()
+        u0, s0, strength = 0.06, 8.0, 0.7
+        flow = lbm.Flow(u0, s0, strength, omega.tack, side)
+        f_in, solid = seeded_state(lbm, geo, n, rng)
+        fields = {key: tack_shim.HostManagedArray(n) for key in lbm.FIELDS}
+        for key in ("ux", "uy", "uz", "p"):
+            fields[key].numpy[:] = (0.02 * rng.standard_normal(n)).astype(np.float32)
+        prev = {key: fields[key].numpy.copy() for key in lbm.FIELDS}
+        diag = (lbm.Report if report else lbm.Quiet)({k_: v.tack for k_, v in fields.items()})
+        h = heat_stub(lbm, n)
+        a_in = lbm.tack.array(f_in)
+        a_out = lbm.tack.empty((19 * n,))
+        t0 = time.perf_counter()
+        lbm.lbm_step(lat, phys, geo, flow, diag, a_in, a_out, h.heat, h.g[0], h.g[1])
+        print(f"{name}: {time.perf_counter() - t0:.2f} s, solid cells {int(solid.sum())}")
+        out[f"{name}/f_in"] = f_in
+        out[f"{name}/f_out"] = np.asarray(a_out)
+        out[f"{name}/solid"] = solid.astype(np.uint8)
+        for key in lbm.FIELDS:
+            out[f"{name}/prev/{key}"] = prev[key].astype(np.float32)
+            if report:
+                out[f"{name}/fields/{key}"] = np.asarray(fields[key].numpy)
+        meta[name] = dict(nx=NX, ny=NY, nz=NZ, collision=coll, nu=nu, obstacle=obst, lateral=lateral,
+                          report=report, omega_rot=omega_rot, u0=u0, sponge_start=s0,
+                          sponge_strength=strength, **GEOMETRY[obst])
+    out["meta"] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(HERE, "step_cases.npz"), **out)
+
+
+def make_init_cases(ref_dir):
+    lbm = tack_shim.import_reference(ref_dir)
+    n = NX * NY * NZ
+    out, meta = {}, {}
+    for obst in GEOMETRY:
+        lat = lbm.D3Q19(NX, NY, NZ)
+        geo = geometry(lbm, obst)
+        flow = lbm.Flow(0.07, 9.0, 1.0)
+        f = lbm.tack.empty((19 * n,))
+        lbm.lbm_init(lat, geo, flow, f, 0.05)
+        out[f"{obst}/f"] = np.asarray(f)
+        meta[obst] = dict(nx=NX, ny=NY, nz=NZ, obstacle=obst, u0=0.07, seed_amp=0.05, **GEOMETRY[obst])
+    out["meta"] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(HERE, "init_cases.npz"), **out)
+
+
+def make_solver_cases(ref_dir):
+    lbm = tack_shim.import_reference(ref_dir)
+    out, meta = {}, {}
+    for case in SOLVER_CASES:
+        c = dict(case)
+        name, rotation = c.pop("name"), c.pop("rotation")
+        t0 = time.perf_counter()
+        s = lbm.Solver(**c)
+        mon0 = s.monitors(1)
+        s.set_actuation(rotation)
+        for _ in range(3):
+            s.step()
+        s.step(report=True)
+        mon1 = s.monitors(4)
+        s.step()
+        s.step(report=True)
+        mon2 = s.monitors(2)
+        print(f"solver {name}: {time.perf_counter() - t0:.1f} s, steps {s.step_count}, "
+              f"drag {mon2['drag']:.5f} lift {mon2['lift']:.5f}")
+        out[f"{name}/f"] = np.asarray(s.f[0])
+        out[f"{name}/solid"] = np.array([s.geo.solid(i % s.nx, (i // s.nx) % s.ny, i // (s.nx * s.ny))
+                                         for i in range(s.lat.n)], np.uint8)
+        for key in lbm.FIELDS:
+            out[f"{name}/fields/{key}"] = np.asarray(s.fields[key].numpy)
+        meta[name] = dict(case, monitors=[mon0, mon1, mon2], step_count=s.step_count,
+                          nu=s.nu, sponge_start=s.flow.sponge_start)
+    out["meta"] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(HERE, "solver_cases.npz"), **out)
+
+
+def main():
+    ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    make_trt_ref(ref_dir)
+    make_step_cases(ref_dir)
+    make_init_cases(ref_dir)
+    make_solver_cases(ref_dir)
+
+
+if __name__ == "__main__":
+    main()

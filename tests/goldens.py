@@ -1,0 +1,41 @@
+"""Loaders for the golden vectors in tests/golden/ (made by make_golden.py)."""
+
+import json
+import os
+
+import numpy as np
+
+from oracle import lbm_oracle as O
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    meta = json.loads(str(z["meta"])) if "meta" in z.files else None
+    return z, meta
+
+
+def trt_ref_config():
+    """trt_ref.py:27-29: TRT(0.002), Cylinder(-100, -100, 0), Flow(0, 1e9, 0)."""
+    z, _ = load("trt_ref")
+    nx, ny, nz = (int(v) for v in z["dims"])
+    return O.Config(nx, ny, nz, collision="trt", nu=float(z["nu"]), obstacle="cylinder",
+                    ox=-100.0, oy=-100.0, r=0.0, u0=0.0, sponge_start=1e9, sponge_strength=0.0)
+
+
+def step_case_config(m):
+    keys = ("collision", "nu", "obstacle", "lateral", "omega_rot", "u0", "sponge_start",
+            "sponge_strength", "ox", "oy", "oz", "r", "hx", "hy", "hz")
+    return O.Config(m["nx"], m["ny"], m["nz"], **{k: m[k] for k in keys if k in m})
+
+
+def step_cases():
+    z, meta = load("step_cases")
+    for name, m in meta.items():
+        case = {"name": name, "cfg": step_case_config(m), "report": m["report"],
+                "f_in": z[f"{name}/f_in"], "f_out": z[f"{name}/f_out"], "solid": z[f"{name}/solid"],
+                "prev": {k: z[f"{name}/prev/{k}"] for k in O.FIELDS}}
+        if m["report"]:
+            case["fields"] = {k: z[f"{name}/fields/{k}"] for k in O.FIELDS}
+        yield case

@@ -1,0 +1,313 @@
+"""Parity of the CUDA step with the oracle and the reference's golden vectors.
+
+Every call goes through the C ABI (liblbm_gb300.so via ctypes). Tolerances:
+
+* one FP32 step: max |f_gpu - f_ref| / w_q <= 1e-6 (each population's error
+  relative to its lattice weight; see test_oracle_golden.py for why the
+  pointwise relative error is not used);
+* FP64 storage: 1e-12 on the same yardstick;
+* FP16 / BF16 deviation storage: the storage quantum (3e-4 / 3e-3);
+* solid masks: bit-exact.
+"""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import lbm_oracle as O
+import goldens
+
+pytestmark = pytest.mark.gpu
+
+TOL32 = 1e-6
+
+
+@pytest.fixture(scope="module")
+def G():
+    import lbm as G  # the drop-in module; loads (and builds) the native library
+    import lbm_native
+    lbm_native.load()
+    return G
+
+
+def native_handle(cfg, storage="f32"):
+    import lbm_native as N
+    c = N.Config()
+    c.nx, c.ny, c.nz = cfg.nx, cfg.ny, cfg.nz
+    c.collision = N.COLLISION[cfg.collision]
+    c.obstacle = N.OBSTACLE[cfg.obstacle]
+    c.lateral = N.SIDE[cfg.lateral]
+    c.vertical = N.SIDE[cfg.vertical]
+    c.storage = N.STORAGE[storage]
+    c.nu, c.cs, c.magic = cfg.nu, cfg.cs, cfg.magic
+    c.ox, c.oy, c.oz, c.r, c.hx, c.hy, c.hz = cfg.ox, cfg.oy, cfg.oz, cfg.r, cfg.hx, cfg.hy, cfg.hz
+    c.u0, c.sponge_start, c.sponge_strength = cfg.u0, cfg.sponge_start, cfg.sponge_strength
+    c.u_lid, c.omega_rot = cfg.u_lid, cfg.omega_rot
+    return N.Handle(c)
+
+
+def put(h, f):
+    import lbm_native as N
+    src = np.ascontiguousarray(f, np.float64).reshape(-1)
+    h.call("lbm_set_populations", src.ctypes.data_as(ctypes.c_void_p), N.F64, N.HOST)
+
+
+def get(h, n):
+    import lbm_native as N
+    out = np.empty(19 * n, np.float64)
+    h.call("lbm_get_populations", out.ctypes.data_as(ctypes.c_void_p), N.F64, N.HOST)
+    return out
+
+
+def get_fields(h, n):
+    h.call("lbm_sync")
+    out = {}
+    for k, name in enumerate(O.FIELDS):
+        ptr = ctypes.c_void_p()
+        h.call("lbm_field", k, ctypes.byref(ptr))
+        out[name] = np.ctypeslib.as_array((ctypes.c_float * n).from_address(ptr.value)).copy()
+    return out
+
+
+def set_fields(h, fields):
+    for k, name in enumerate(O.FIELDS):
+        v = np.ascontiguousarray(fields[name], np.float32)
+        h.call("lbm_set_field", k, v.ctypes.data_as(ctypes.c_void_p))
+
+
+def gpu_mask(h, n):
+    out = np.empty(n, np.uint8)
+    h.call("lbm_mask", out.ctypes.data_as(ctypes.c_void_p))
+    return out
+
+
+def check_fields(got, want, where=""):
+    for k in O.FIELDS:
+        g, w = np.asarray(got[k], np.float64), np.asarray(want[k], np.float64)
+        if k.startswith("r_"):
+            tol = 1e-6 * max(np.abs(w).max(), 1e-12) + 1e-12
+        elif k in ("fx", "fy", "fz"):
+            tol = 2e-6
+        else:
+            tol = 2e-7
+        err = np.abs(g - w).max()
+        assert err <= tol, f"{where} field {k}: max err {err:.3e} > {tol:.3e}"
+
+
+# ---------------------------------------------------------------------------
+
+def test_trt_ref_through_kernel_entry(G):
+    """trt_ref.py (trt_ref.py:8-60) with this module in place of the reference's."""
+    z, _ = goldens.load("trt_ref")
+    nx, ny, nz = (int(v) for v in z["dims"])
+    n = nx * ny * nz
+    lat = G.D3Q19(nx, ny, nz)
+    trt = G.TRT(0.002)
+    geo = G.Cylinder(-100.0, -100.0, 0.0)
+    flow = G.Flow(0.0, 1e9, 0.0)
+    fields = {k: G.ManagedArray(n).tack for k in G.FIELDS}
+    out = np.empty(19 * n, np.float32)
+    G.lbm_step(lat, trt, geo, flow, G.Quiet(fields), z["f_in"], out, G.NoHeat(), None, None)
+    assert O.weight_err(out, z["got"]) <= TOL32
+    assert np.abs(out - z["ref"]).max() < 1e-5          # trt_ref.py's own assertion
+    assert O.weight_err(out, z["ref"]) <= 2e-6           # trt_ref uses exact weights
+
+
+@pytest.mark.parametrize("case", list(goldens.step_cases()), ids=lambda c: c["name"])
+def test_golden_step(G, case):
+    cfg = case["cfg"]
+    h = native_handle(cfg)
+    assert np.array_equal(gpu_mask(h, cfg.n), case["solid"])
+    put(h, case["f_in"])
+    set_fields(h, case["prev"])
+    h.call("lbm_step", int(case["report"]), None)
+    out = get(h, cfg.n)
+    assert O.weight_err(out, case["f_out"]) <= TOL32, case["name"]
+    if case["report"]:
+        check_fields(get_fields(h, cfg.n), case["fields"], case["name"])
+
+
+@pytest.mark.parametrize("case", list(goldens.step_cases()), ids=lambda c: c["name"])
+def test_three_steps_both_parities(G, case):
+    """Odd, even and odd AA steps against three oracle steps (report on the even one)."""
+    cfg = case["cfg"]
+    h = native_handle(cfg)
+    put(h, case["f_in"])
+    set_fields(h, case["prev"])
+    fields = {k: v.astype(np.float64) for k, v in case["prev"].items()}
+    f = case["f_in"].astype(np.float64)
+    for k, rep in enumerate((False, True, False)):
+        h.call("lbm_step", int(rep), None)
+        f = O.step(cfg, f, fields, report=rep).reshape(-1)
+        err = O.weight_err(get(h, cfg.n), f)
+        assert err <= 3 * TOL32, f"{case['name']} step {k + 1}: {err:.3e}"
+        if rep:
+            check_fields(get_fields(h, cfg.n), fields, case["name"])
+
+
+def test_init_golden(G):
+    z, meta = goldens.load("init_cases")
+    for name, m in meta.items():
+        geo = {"cylinder": G.Cylinder(m["ox"], m["oy"], m["r"]),
+               "sphere": G.Sphere(m["ox"], m["oy"], m["oz"], m["r"]),
+               "box": G.Box(m["ox"], m["oy"], m["oz"], m["hx"], m["hy"], m["hz"])}[name]
+        lat = G.D3Q19(m["nx"], m["ny"], m["nz"])
+        f = np.empty(19 * lat.n, np.float32)
+        G.lbm_init(lat, geo, G.Flow(m["u0"], 9.0, 1.0), f, m["seed_amp"])
+        assert O.weight_err(f, z[f"{name}/f"]) <= TOL32, name
+
+
+def test_solver_golden(G):
+    """Whole Solver runs (construction, rotation change, report steps, monitors)."""
+    z, meta = goldens.load("solver_cases")
+    for name, m in meta.items():
+        s = G.Solver(m["nx"], m["ny"], m["nz"], collision=m["collision"], obstacle=m["obstacle"],
+                     reynolds=m["reynolds"], u0=m["u0"], diameter=m["diameter"], lateral=m["lateral"])
+        assert s.nu == m["nu"] and s.flow.sponge_start == m["sponge_start"]
+        assert np.array_equal(s.mask(), z[f"{name}/solid"])
+        mons = [s.monitors(1)]
+        s.set_actuation(m["rotation"])
+        for _ in range(3):
+            s.step()
+        s.step(report=True)
+        mons.append(s.monitors(4))
+        s.step()
+        s.step(report=True)
+        mons.append(s.monitors(2))
+        assert s.step_count == m["step_count"]
+        assert O.weight_err(s.populations(), z[f"{name}/f"]) <= 1e-5, name
+        for got, want in zip(mons, m["monitors"]):
+            for k, v in want.items():
+                assert got[k] == pytest.approx(v, rel=2e-5, abs=1e-9), (name, k, got[k], v)
+        fields = {k: s.fields[k].numpy.copy() for k in O.FIELDS}
+        check_fields(fields, {k: z[f"{name}/fields/{k}"] for k in O.FIELDS}, name)
+
+
+def c1_config(cs):
+    """64x32x16 plain TRT cylinder: r = 4 at (16, 16), Re 300 at U = 0.08, sponge over 8 planes."""
+    return O.Config(64, 32, 16, collision="trt", nu=0.08 * 8 / 300, cs=cs, obstacle="cylinder",
+                    ox=16.0, oy=16.0, r=4.0, u0=0.08, sponge_start=56.0, sponge_strength=1.0)
+
+
+@pytest.mark.parametrize("cs", [0.0, 0.16])
+def test_c1_one_step_and_200_steps(G, cs):
+    cfg = c1_config(cs)
+    h = native_handle(cfg)
+    h.call("lbm_init_random", 1e-3, 0.01, 2024)
+    f0 = get(h, cfg.n)
+    assert O.weight_err(f0, O.init_random(cfg, 1e-3, 0.01, 2024)) <= TOL32
+    assert np.array_equal(gpu_mask(h, cfg.n), O.mask(cfg).astype(np.uint8))
+    h.call("lbm_step", 0, None)
+    f1 = O.step(cfg, f0).reshape(-1)
+    assert O.weight_err(get(h, cfg.n), f1) <= TOL32
+    h.call("lbm_run", 199, 0, None)
+    f = O.run(cfg, f1, 199)
+    err = O.weight_err(get(h, cfg.n), f)
+    # 200 float32 steps against float64: round-off accumulates, the flow does not diverge
+    assert err <= 2e-5, err
+
+
+def test_storage_variants(G):
+    case = next(c for c in goldens.step_cases() if c["name"] == "les_sphere_slip_report")
+    cfg = case["cfg"]
+    want = case["f_out"]
+    for storage, tol in (("f64", 1e-12), ("f16", 3e-4), ("bf16", 3e-3)):
+        h = native_handle(cfg, storage)
+        put(h, case["f_in"])
+        set_fields(h, case["prev"])
+        h.call("lbm_step", 1, None)
+        if storage == "f64":
+            assert O.weight_err(get(h, cfg.n), want) <= tol
+        else:
+            # the input itself is quantized by the storage; compare with the oracle on that input
+            h2 = native_handle(cfg, storage)
+            put(h2, case["f_in"])
+            fq = get(h2, cfg.n)
+            ref = O.step(cfg, fq, {k: v.astype(np.float64) for k, v in case["prev"].items()}, report=True)
+            assert O.weight_err(get(h, cfg.n), ref) <= tol, storage
+
+
+@pytest.mark.parametrize("lateral,vertical,obstacle", [
+    ("slip", "slip", "cylinder"), ("lid", "slip", "box"), ("lid", "periodic", "sphere"),
+    ("periodic", "slip", "sphere"), ("lid", "slip", "none")])
+def test_boundary_extensions(G, lateral, vertical, obstacle):
+    """Slip z-walls and the moving lid against the oracle, obstacles touching the walls."""
+    geo = {"cylinder": dict(ox=9.4, oy=6.2, r=3.1),
+           "box": dict(ox=9.5, oy=9.0, oz=2.5, hx=2.5, hy=2.2, hz=4.0),
+           "sphere": dict(ox=10.2, oy=8.6, oz=1.5, r=3.3),
+           "none": {}}[obstacle]
+    cfg = O.Config(36, 11, 7, collision="les", nu=0.01, obstacle=obstacle, u0=0.06,
+                   sponge_start=28.0, sponge_strength=0.8, lateral=lateral, vertical=vertical,
+                   u_lid=0.05, omega_rot=0.02 if obstacle == "cylinder" else 0.0, **geo)
+    h = native_handle(cfg)
+    assert np.array_equal(gpu_mask(h, cfg.n), O.mask(cfg).astype(np.uint8))
+    h.call("lbm_init_random", 1e-3, 0.01, 7)
+    f = get(h, cfg.n)
+    fields = O.new_fields(cfg.n)
+    for k in range(6):
+        rep = k in (2, 5)
+        h.call("lbm_step", int(rep), None)
+        f = O.step(cfg, f, fields, report=rep).reshape(-1)
+        err = O.weight_err(get(h, cfg.n), f)
+        assert err <= 3 * TOL32, f"step {k + 1}: {err:.3e}"
+        if rep:
+            check_fields(get_fields(h, cfg.n), fields, f"step {k + 1}")
+
+
+def test_set_obstacle_and_physics_midrun(G):
+    """Changing the model, viscosity, obstacle and rotation between steps (lbm.py:613-637)."""
+    cfg = O.solver_config(48, 24, 8, collision="les", obstacle="cylinder", reynolds=200.0,
+                          u0=0.07, diameter=6.0, lateral="slip")
+    s = G.Solver(48, 24, 8, collision="les", obstacle="cylinder", reynolds=200.0, u0=0.07,
+                 diameter=6.0, lateral="slip")
+    f = s.populations(np.float64)
+    for _ in range(3):
+        s.step()
+        f = O.step(cfg, f).reshape(-1)
+    s.set_physics("trt", 500.0)
+    cfg.collision, cfg.nu = "trt", s.nu
+    s.set_actuation(0.03)
+    cfg.omega_rot = 0.03
+    for _ in range(2):
+        s.step()
+        f = O.step(cfg, f).reshape(-1)
+    assert O.weight_err(s.populations(), f) <= 3e-6
+    s.set_obstacle("sphere")
+    cfg.obstacle, cfg.oz = "sphere", 4.0
+    fsolid = O.mask(cfg) > 0
+    f = f.reshape(19, -1)
+    f[:, fsolid] = O.W[:, None]   # the carried-over populations, solid cells at rest
+    f = f.reshape(-1)
+    for _ in range(3):
+        s.step()
+        f = O.step(cfg, f).reshape(-1)
+    assert np.array_equal(s.mask(), O.mask(cfg).astype(np.uint8))
+    assert O.weight_err(s.populations(), f) <= 5e-6
+
+
+def test_output_stride(G):
+    s = G.Solver(40, 20, 10, collision="les", obstacle="sphere", diameter=6.0, stride=3)
+    assert s.out_dims == (14, 7, 4)
+    for _ in range(3):
+        s.step()
+    s.step(report=True)
+    s.monitors(4)
+    for name in s.OUTPUT:
+        full = s.fields[name].numpy.reshape(10, 20, 40)
+        assert np.array_equal(s.output[name].numpy.reshape(4, 7, 14), full[::3, ::3, ::3]), name
+
+
+def test_nonfinite_monitors_reported(G):
+    """A diverged run gives non-finite monitors instead of raising (collision_check.py:19)."""
+    cfg = O.Config(32, 8, 4, collision="bgk", nu=0.01, obstacle="none", u0=0.05,
+                   sponge_start=1e9, sponge_strength=0.0)
+    h = native_handle(cfg)
+    f = O.init(cfg, 0.0)
+    f[5 * cfg.n + 3] = np.nan
+    put(h, f)
+    h.call("lbm_step", 1, None)
+    import lbm_native as N
+    out = (ctypes.c_double * 7)()
+    status = h.call("lbm_monitors", 1, 8.0, out, allow=(N.ERR_NONFINITE,))
+    assert status == N.ERR_NONFINITE and not np.isfinite(out[0])

@@ -1,0 +1,121 @@
+"""Pin the NumPy oracle against vectors produced by the reference itself.
+
+The fixtures come from tack-lbm's own ``lbm.py`` kernels executed as Python
+(tests/golden/make_golden.py) and from ``trt_ref.py``'s NumPy TRT step. In
+float64 the oracle must reproduce them to round-off.
+"""
+
+import numpy as np
+import pytest
+
+from oracle import lbm_oracle as O
+import goldens
+
+RTOL64 = 1e-12
+
+
+def rel_err(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.max(np.abs(a - b) / (np.abs(b) + 1e-30))) if a.size else 0.0
+
+
+def test_lattice_tables():
+    # lbm.py:15-18 ordering, opposite and mirror tables (lbm.py:28-35)
+    assert O.CX.sum() == O.CY.sum() == O.CZ.sum() == 0
+    c = np.stack([O.CX, O.CY, O.CZ], 1)
+    assert (c[O.OPP] == -c).all()
+    assert (c[O.MIRY] == c * [1, -1, 1]).all()
+    assert (c[O.MIRZ] == c * [1, 1, -1]).all()
+    assert O.W.dtype == np.float64 and np.all(O.W == O.W.astype(np.float32))
+    assert abs(O.W.sum() - 1.0) < 1e-7
+
+
+def test_trt_ref_numpy_and_kernel():
+    z, _ = goldens.load("trt_ref")
+    cfg = goldens.trt_ref_config()
+    out = O.step(cfg, z["f_in"]).reshape(-1)
+    # the reference kernel (float32 weights, lbm.py:48) to round-off
+    assert np.max(np.abs(out - z["got"])) < 1e-15
+    # trt_ref.py's NumPy step uses exact weights: within its own assertion and 1e-6 relative
+    assert np.max(np.abs(out - z["ref"])) < 1e-5
+    assert rel_err(out, z["ref"]) < 1e-6
+
+
+@pytest.mark.parametrize("case", list(goldens.step_cases()), ids=lambda c: c["name"])
+def test_step_cases(case):
+    cfg = case["cfg"]
+    fields = {k: v.astype(np.float64) for k, v in case["prev"].items()}
+    out = O.step(cfg, case["f_in"], fields, report=case["report"]).reshape(-1)
+    assert rel_err(out, case["f_out"]) < RTOL64
+    assert np.array_equal(O.mask(cfg).astype(np.uint8), case["solid"])
+    assert np.array_equal(O.mask(cfg, "f32").astype(np.uint8), case["solid"])
+    if case["report"]:
+        for k in O.FIELDS:
+            np.testing.assert_allclose(fields[k], case["fields"][k], rtol=1e-11, atol=1e-15, err_msg=k)
+
+
+def test_init_cases():
+    z, meta = goldens.load("init_cases")
+    for name, m in meta.items():
+        geo = {k: m[k] for k in ("ox", "oy", "oz", "r", "hx", "hy", "hz") if k in m}
+        cfg = O.Config(m["nx"], m["ny"], m["nz"], obstacle=m["obstacle"], u0=m["u0"], **geo)
+        f = O.init(cfg, m["seed_amp"])
+        assert rel_err(f, z[f"{name}/f"]) < RTOL64, name
+
+
+def run_solver_case(m):
+    """Replay make_golden.py's Solver script on the oracle (lbm.py:551-661)."""
+    cfg = O.solver_config(m["nx"], m["ny"], m["nz"], collision=m["collision"], obstacle=m["obstacle"],
+                          reynolds=m["reynolds"], u0=m["u0"], diameter=m["diameter"], lateral=m["lateral"])
+    fields = O.new_fields(cfg.n)
+    f = O.init(cfg, 0.05)
+    f = O.step(cfg, f, fields, report=True).reshape(-1)
+    mons = [O.monitors(cfg, fields, 1, m["diameter"])]
+    cfg.omega_rot = m["rotation"]
+    for _ in range(3):
+        f = O.step(cfg, f).reshape(-1)
+    f = O.step(cfg, f, fields, report=True).reshape(-1)
+    mons.append(O.monitors(cfg, fields, 4, m["diameter"]))
+    f = O.step(cfg, f).reshape(-1)
+    f = O.step(cfg, f, fields, report=True).reshape(-1)
+    mons.append(O.monitors(cfg, fields, 2, m["diameter"]))
+    return cfg, f, fields, mons
+
+
+def test_solver_cases():
+    z, meta = goldens.load("solver_cases")
+    for name, m in meta.items():
+        cfg, f, fields, mons = run_solver_case(m)
+        assert cfg.nu == m["nu"] and cfg.sponge_start == m["sponge_start"]
+        assert np.array_equal(O.mask(cfg).astype(np.uint8), z[f"{name}/solid"])
+        assert np.array_equal(O.mask(cfg, "f32").astype(np.uint8), z[f"{name}/solid"])
+        assert rel_err(f, z[f"{name}/f"]) < 1e-11, name
+        for k in O.FIELDS:
+            np.testing.assert_allclose(fields[k], z[f"{name}/fields/{k}"], rtol=1e-9, atol=1e-14,
+                                       err_msg=f"{name}/{k}")
+        for got, want in zip(mons, m["monitors"]):
+            for k, v in want.items():
+                assert got[k] == pytest.approx(v, rel=1e-9, abs=1e-14), (name, k)
+
+
+def weight_err(a, b):
+    """max |a - b| / w_q: the error of each population relative to its lattice weight."""
+    d = np.abs(np.asarray(a, np.float64).reshape(19, -1) - np.asarray(b, np.float64).reshape(19, -1))
+    return float((d / O.W[:, None]).max())
+
+
+def test_float32_mode_close_to_float64():
+    """The reference's own arithmetic in float32 stays within 1e-6 of the
+    float64 result when each population's error is scaled by its weight.
+    (Pointwise relative error is not a usable yardstick: trt_ref's random
+    velocities make some populations a tenth of their weight, where float32
+    round-off alone reaches 2e-6.)"""
+    z, _ = goldens.load("trt_ref")
+    cfg = goldens.trt_ref_config()
+    out32 = O.step(cfg, z["f_in"], dtype=np.float32).reshape(-1)
+    assert out32.dtype == np.float32
+    assert weight_err(out32, z["got"]) < 1e-6
+    for case in goldens.step_cases():
+        fields = {k: v.astype(np.float32) for k, v in case["prev"].items()}
+        out = O.step(case["cfg"], case["f_in"], fields, report=case["report"], dtype=np.float32)
+        assert weight_err(out, case["f_out"]) < 1e-6, case["name"]
