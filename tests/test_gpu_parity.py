@@ -86,7 +86,9 @@ def check_fields(got, want, where=""):
     for k in O.FIELDS:
         g, w = np.asarray(got[k], np.float64), np.asarray(want[k], np.float64)
         if k.startswith("r_"):
-            tol = 1e-6 * max(np.abs(w).max(), 1e-12) + 1e-12
+            # r = a^2 with a a float32 difference good to ~1e-7: |dr| <= 2 |a| da
+            big = np.abs(w).max()
+            tol = 2e-7 * np.sqrt(big) + 1e-6 * big + 1e-14
         elif k in ("fx", "fy", "fz"):
             tol = 2e-6
         else:
@@ -149,9 +151,9 @@ def test_three_steps_both_parities(G, case):
 def test_init_golden(G):
     z, meta = goldens.load("init_cases")
     for name, m in meta.items():
-        geo = {"cylinder": G.Cylinder(m["ox"], m["oy"], m["r"]),
-               "sphere": G.Sphere(m["ox"], m["oy"], m["oz"], m["r"]),
-               "box": G.Box(m["ox"], m["oy"], m["oz"], m["hx"], m["hy"], m["hz"])}[name]
+        geo = {"cylinder": lambda: G.Cylinder(m["ox"], m["oy"], m["r"]),
+               "sphere": lambda: G.Sphere(m["ox"], m["oy"], m["oz"], m["r"]),
+               "box": lambda: G.Box(m["ox"], m["oy"], m["oz"], m["hx"], m["hy"], m["hz"])}[name]()
         lat = G.D3Q19(m["nx"], m["ny"], m["nz"])
         f = np.empty(19 * lat.n, np.float32)
         G.lbm_init(lat, geo, G.Flow(m["u0"], 9.0, 1.0), f, m["seed_amp"])
@@ -201,11 +203,23 @@ def test_c1_one_step_and_200_steps(G, cs):
     h.call("lbm_step", 0, None)
     f1 = O.step(cfg, f0).reshape(-1)
     assert O.weight_err(get(h, cfg.n), f1) <= TOL32
-    h.call("lbm_run", 199, 0, None)
-    f = O.run(cfg, f1, 199)
-    err = O.weight_err(get(h, cfg.n), f)
-    # 200 float32 steps against float64: round-off accumulates, the flow does not diverge
-    assert err <= 2e-5, err
+    if cs > 0:
+        # with the subgrid viscosity the flow is stable: 200 float32 steps against float64
+        h.call("lbm_run", 199, 0, None)
+        f = O.run(cfg, f1, 199)
+        err = O.weight_err(get(h, cfg.n), f)
+        assert err <= 2e-5, err
+        return
+    # plain TRT at Re 300 is unstable (lbm.py:99-101: beyond Re ~100): compare the
+    # first 60 steps, then both runs must have blown up by step 200
+    h.call("lbm_run", 59, 0, None)
+    f = O.run(cfg, f1, 59)
+    assert O.weight_err(get(h, cfg.n), f) <= 2e-5
+    h.call("lbm_run", 140, 0, None)
+    with np.errstate(all="ignore"):
+        f = O.run(cfg, f, 140)
+        g = get(h, cfg.n)
+        assert not (np.abs(f).max() < 10.0) and not (np.abs(g).max() < 10.0)
 
 
 def test_storage_variants(G):
