@@ -185,6 +185,25 @@ lbm_status lbm_timing_read(lbm_solver *s, double out[7]);
 /* Synchronise the solver's device work (tack.sync, lbm.py:651). */
 lbm_status lbm_sync(lbm_solver *s);
 
+/* Largest n accepted by lbm_field_sums_static: 2^28 cells. */
+#define LBM_STATIC_SUMS_MAX_CELLS 268435456LL
+
+/* The eight FP64 monitor sums (r_rho, r_ux, r_uy, r_uz, r_ke, fx, fy, fz, the
+ * totals Solver.monitors turns into residuals and drag/lift) of caller-owned
+ * report fields, WITHOUT ANY DEVICE ALLOCATION. There is no counterpart in the
+ * reference. It exists for callers that cannot allocate device memory while
+ * they run: an in-situ pipeline or host framework that owns every device
+ * buffer and forbids allocation mid-run (cudaMalloc synchronises the device and
+ * can fail under memory pressure), or a deployment with a fixed device
+ * footprint. fields: 8 arrays of n floats the GPU can read (device or
+ * managed memory); sums: 8 doubles the GPU can write. n must be in
+ * [1, LBM_STATIC_SUMS_MAX_CELLS], otherwise LBM_ERR_ARG. Runs asynchronously on
+ * `stream` of the current device. The per-block partial sums go to a static
+ * 1 MiB device array that every GPU loading the library holds until exit; the
+ * first call on a device looks up that array's address, so make it before any
+ * stream capture. All calls share the array: calls that overlap on the GPU race. */
+lbm_status lbm_field_sums_static(const float *const fields[8], int64_t n, double *sums, void *stream);
+
 /* Message of the last error on this thread ("" when none). */
 const char *lbm_last_error(void);
 

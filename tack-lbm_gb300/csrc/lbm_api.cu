@@ -239,6 +239,8 @@ void release(lbm_solver *s) {
 
 namespace lbmh {
 
+void set_last_error(const std::string &msg) { g_err = msg; }
+
 __global__ void finalize_stage(const double *partials, int64_t nb, double *stage) {
   __shared__ double sm[256][lbmk::NSUM];
   const int64_t chunk = (nb + gridDim.x - 1) / gridDim.x;

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 #include "../../include/lbm_gb300.h"
 
 namespace lbmh {
@@ -47,5 +49,8 @@ template <typename S> cudaError_t launch_export(const Ctx &c, void *dst, int dty
 cudaError_t launch_finalize(const Ctx &c, cudaStream_t st);
 cudaError_t launch_mask(const Ctx &c, uint8_t *dst_dev, cudaStream_t st);
 cudaError_t launch_coarsen(const Ctx &c, cudaStream_t st);
+
+// message returned by lbm_last_error() on this thread
+void set_last_error(const std::string &msg);
 
 }  // namespace lbmh

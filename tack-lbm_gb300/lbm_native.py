@@ -80,6 +80,8 @@ _SIGNATURES = {
     "lbm_sync": (ctypes.c_int, [ctypes.c_void_p]),
     "lbm_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "lbm_timing_read": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
+    "lbm_field_sums_static": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int64,
+                                             ctypes.c_void_p, ctypes.c_void_p]),
     "lbm_managed_alloc": (ctypes.c_int, [ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
     "lbm_managed_free": (ctypes.c_int, [ctypes.c_void_p]),
 }
