@@ -80,8 +80,13 @@ typedef struct lbm_config {
     double u_lid;                /* x velocity of the LBM_LID top wall */
     double omega_rot;            /* cylinder surface speed (lbm.py:618-620) */
     int32_t device;              /* CUDA device ordinal */
-    int32_t reserved;
+    int32_t flags;               /* LBM_FLAG_* */
 } lbm_config;
+
+/* lbm_config.flags: use the per-cell kernels instead of the bulk-copy kernel
+ * (which needs nx*sizeof(storage) in 16-byte pieces; without them the per-cell
+ * kernels are used anyway). */
+#define LBM_FLAG_SIMT 1
 
 typedef struct lbm_solver lbm_solver;
 

@@ -18,6 +18,7 @@
 
 #include "lbm_device.cuh"
 #include "lbm_host.h"
+#include "lbm_stream.cuh"
 
 using lbmh::Ctx;
 
@@ -155,6 +156,47 @@ lbm_status classify_blocks(lbm_solver *s) {
   return LBM_OK;
 }
 
+// Row segments of the bulk-copy kernel within reach of the obstacle get link masks.
+lbm_status classify_segments(lbm_solver *s) {
+  Ctx &c = s->c;
+  const lbm_config &g = c.cfg;
+  cudaFree(c.seg_mask);
+  cudaFree(c.seg_list);
+  cudaFree(c.masks);
+  c.seg_mask = nullptr;
+  c.seg_list = nullptr;
+  c.masks = nullptr;
+  c.nmasked = 0;
+  if (!c.use_stream) return LBM_OK;
+  Range box[3];
+  bool any;
+  obstacle_box(g, box, any);
+  std::vector<int> slot((size_t)c.nseg, -1), list;
+  for (int z = 0; z < g.nz; ++z)
+    for (int y = 0; y < g.ny; ++y)
+      for (int sx = 0; sx < c.nseg_x; ++sx) {
+        const int64_t x0 = (int64_t)sx * lbmk::SW;
+        const int64_t x1 = std::min<int64_t>(x0 + lbmk::SW, g.nx) - 1;
+        if (any && x1 >= box[0].lo && x0 <= box[0].hi && y >= box[1].lo && y <= box[1].hi &&
+            z >= box[2].lo && z <= box[2].hi) {
+          const int seg = (z * g.ny + y) * c.nseg_x + sx;
+          slot[(size_t)seg] = (int)list.size() * lbmk::SW;
+          list.push_back(seg);
+        }
+      }
+  c.nmasked = (int)list.size();
+  LBM_CUDA(cudaMalloc(&c.seg_mask, slot.size() * sizeof(int)));
+  LBM_CUDA(cudaMemcpy(c.seg_mask, slot.data(), slot.size() * sizeof(int), cudaMemcpyHostToDevice));
+  LBM_CUDA(cudaMalloc(&c.seg_list, std::max<size_t>(1, list.size()) * sizeof(int)));
+  LBM_CUDA(cudaMalloc(&c.masks, std::max<size_t>(1, list.size()) * lbmk::SW * sizeof(uint32_t)));
+  if (!list.empty()) {
+    LBM_CUDA(cudaMemcpy(c.seg_list, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice));
+    LBM_CUDA(lbmh::launch_link_masks<float>(c, 0));
+    LBM_CUDA(cudaDeviceSynchronize());
+  }
+  return LBM_OK;
+}
+
 cudaError_t dispatch_step(const Ctx &c, bool report, cudaStream_t st) {
   switch (c.cfg.storage) {
     case LBM_F16: return lbmh::launch_step<__half>(c, report, st);
@@ -223,6 +265,10 @@ void release(lbm_solver *s) {
   Ctx &c = s->c;
   release_timing(c);
   release_output(c);
+  cudaFree(c.seg_mask);
+  cudaFree(c.seg_list);
+  cudaFree(c.masks);
+  cudaFree(c.error);
   cudaFree(c.F);
   for (int k = 0; k < LBM_NUM_FIELDS; ++k) cudaFree(c.fld[k]);
   cudaFree(c.partials);
@@ -267,8 +313,8 @@ __global__ void finalize_last(const double *stage, int g, double *sums) {
   }
 }
 
-cudaError_t launch_finalize(const Ctx &c, cudaStream_t st) {
-  finalize_stage<<<FINALIZE_BLOCKS, 256, 0, st>>>(c.partials, c.nblocks, c.stage);
+cudaError_t launch_finalize(const Ctx &c, int64_t rows, cudaStream_t st) {
+  finalize_stage<<<FINALIZE_BLOCKS, 256, 0, st>>>(c.partials, rows, c.stage);
   finalize_last<<<1, 32, 0, st>>>(c.stage, FINALIZE_BLOCKS, c.sums);
   return cudaGetLastError();
 }
@@ -341,6 +387,22 @@ lbm_status lbm_create(const lbm_config *cfg, lbm_solver **out) {
   c.nblocks = (int64_t)c.gx * c.gy * cfg->nz;
   c.odd_next = 1;
   c.omega_rot = cfg->omega_rot;
+  {
+    // the bulk-copy kernel moves 16-byte pieces: rows must split into them
+    const int h = 16 / (int)storage_bytes(cfg->storage);
+    const int tail = cfg->nx % lbmk::SW;
+    c.use_stream = !(cfg->flags & LBM_FLAG_SIMT) && cfg->nx % h == 0 && cfg->nx >= 2 * h &&
+                   (tail == 0 || tail >= 2 * h);
+    c.nseg_x = (cfg->nx + lbmk::SW - 1) / lbmk::SW;
+    c.nseg = c.nseg_x * cfg->ny * cfg->nz;
+  }
+  {
+    cudaError_t e0 = cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, cfg->device);
+    if (e0 != cudaSuccess) {
+      delete s;
+      return fail(LBM_ERR_CUDA, std::string("cudaDeviceGetAttribute: ") + cudaGetErrorString(e0));
+    }
+  }
   auto bail = [&](lbm_status e) {
     release(s);
     delete s;
@@ -356,14 +418,20 @@ lbm_status lbm_create(const lbm_config *cfg, lbm_solver **out) {
     if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("cudaMallocManaged: ") + cudaGetErrorString(e)));
     s->bytes += c.n * (int64_t)sizeof(float);
   }
-  e = cudaMalloc(&c.partials, (size_t)c.nblocks * lbmk::NSUM * sizeof(double));
+  c.partial_rows = std::max<int64_t>(c.nblocks, (int64_t)c.num_sms * 32);
+  e = cudaMalloc(&c.partials, (size_t)c.partial_rows * lbmk::NSUM * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&c.error, sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMemset(c.error, 0, sizeof(unsigned int));
   if (e == cudaSuccess) e = cudaMalloc(&c.stage, lbmh::FINALIZE_BLOCKS * lbmk::NSUM * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&c.sums, lbmk::NSUM * sizeof(double));
   if (e == cudaSuccess) e = cudaMemset(c.sums, 0, lbmk::NSUM * sizeof(double));
   if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("scratch: ") + cudaGetErrorString(e)));
-  s->bytes += (c.nblocks + lbmh::FINALIZE_BLOCKS + 1) * lbmk::NSUM * (int64_t)sizeof(double);
+  s->bytes += (c.partial_rows + lbmh::FINALIZE_BLOCKS + 1) * lbmk::NSUM * (int64_t)sizeof(double);
   st = classify_blocks(s);
   if (st != LBM_OK) return bail(st);
+  st = classify_segments(s);
+  if (st != LBM_OK) return bail(st);
+  s->bytes += (int64_t)c.nseg * 4 + (int64_t)c.nmasked * (lbmk::SW + 1) * 4;
   s->bytes += c.nblocks + (int64_t)c.nspecial * 4;
   release_output(c);
   e = cudaDeviceSynchronize();
@@ -429,10 +497,22 @@ lbm_status lbm_run(lbm_solver *s, int32_t count, int32_t report_last, void *stre
   return LBM_OK;
 }
 
+static lbm_status check_kernel_error(lbm_solver *s) {
+  unsigned int flag = 0;
+  LBM_CUDA(cudaDeviceSynchronize());
+  LBM_CUDA(cudaMemcpy(&flag, s->c.error, sizeof(flag), cudaMemcpyDeviceToHost));
+  if (flag) {
+    cudaMemset(s->c.error, 0, sizeof(flag));
+    return fail(LBM_ERR_CUDA, "a step kernel gave up waiting for its copies; the populations are invalid");
+  }
+  return LBM_OK;
+}
+
 lbm_status lbm_field_sums(lbm_solver *s, double out[8]) {
   LBM_HANDLE(s);
   if (!out) return fail(LBM_ERR_ARG, "null output");
-  LBM_CUDA(cudaDeviceSynchronize());
+  lbm_status ks = check_kernel_error(s);
+  if (ks != LBM_OK) return ks;
   LBM_CUDA(cudaMemcpy(out, s->c.sums, lbmk::NSUM * sizeof(double), cudaMemcpyDeviceToHost));
   return LBM_OK;
 }
@@ -581,6 +661,7 @@ lbm_status lbm_set_obstacle(lbm_solver *s, int32_t kind, const double geo[7]) {
   }
   s->c.cfg = g;
   st = classify_blocks(s);
+  if (st == LBM_OK) st = classify_segments(s);
   if (st == LBM_OK) {
     s->c.odd_next = 1;
     e = dispatch_import(s->c, tmp, dtype, 0);
@@ -705,6 +786,7 @@ lbm_status lbm_timing(lbm_solver *s, int32_t enable) {
     const int64_t wy = std::min(lbmk::BY, c.cfg.ny - by * lbmk::BY);
     gen += wx * wy;
   }
+  if (c.use_stream) gen = 0;
   c.generic_cells = gen;
   c.bulk_cells = c.n - gen;
   return LBM_OK;
@@ -730,15 +812,14 @@ lbm_status lbm_timing_read(lbm_solver *s, double out[7]) {
   out[1] = c.ev_used;
   out[2] = (double)c.bulk_cells;
   out[3] = gen;
-  out[4] = c.nspecial > 0 ? c.ev_used : 0;
+  out[4] = (c.nspecial > 0 && !c.use_stream) ? c.ev_used : 0;
   out[5] = (double)c.generic_cells;
   return LBM_OK;
 }
 
 lbm_status lbm_sync(lbm_solver *s) {
   LBM_HANDLE(s);
-  LBM_CUDA(cudaDeviceSynchronize());
-  return LBM_OK;
+  return check_kernel_error(s);
 }
 
 }  // extern "C"

@@ -33,6 +33,16 @@ struct Ctx {
   cudaEvent_t *ev;           // 3 events per step in a ring (bulk start, bulk end/generic start, generic end)
   int ev_cap, ev_used;
   int64_t bulk_cells, generic_cells;
+  // bulk-copy (TMA) path: row segments of lbmk::SW cells
+  int use_stream;            // 1 when nx suits 16-byte row pieces
+  int nseg_x, nseg;          // segments per row, segments in the lattice
+  int *seg_mask;             // per segment: first link-mask word or -1
+  int *seg_list;             // the masked segments
+  uint32_t *masks;           // SW words per masked segment
+  int nmasked;
+  unsigned int *error;       // set by a kernel whose copy wait gave up
+  int num_sms;
+  int64_t partial_rows;      // capacity of `partials` in rows of 8 doubles
 };
 
 constexpr int FINALIZE_BLOCKS = 128;
@@ -45,8 +55,9 @@ template <typename S> cudaError_t launch_init_random(const Ctx &c, double rho_si
 // src/dst: device pointers to 19*n values of float (dtype LBM_F32) or double (LBM_F64)
 template <typename S> cudaError_t launch_import(const Ctx &c, const void *src, int dtype, cudaStream_t st);
 template <typename S> cudaError_t launch_export(const Ctx &c, void *dst, int dtype, cudaStream_t st);
+template <typename S> cudaError_t launch_link_masks(const Ctx &c, cudaStream_t st);
 
-cudaError_t launch_finalize(const Ctx &c, cudaStream_t st);
+cudaError_t launch_finalize(const Ctx &c, int64_t rows, cudaStream_t st);
 cudaError_t launch_mask(const Ctx &c, uint8_t *dst_dev, cudaStream_t st);
 cudaError_t launch_coarsen(const Ctx &c, cudaStream_t st);
 

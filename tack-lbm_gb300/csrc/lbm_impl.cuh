@@ -3,6 +3,7 @@
 
 #include "lbm_device.cuh"
 #include "lbm_host.h"
+#include "lbm_stream.cuh"
 
 namespace lbmh {
 
@@ -41,38 +42,78 @@ StepArgs<S> make_args(const Ctx &c) {
   return a;
 }
 
+// Persistent grid of the bulk-copy kernel: every SM filled to its occupancy.
 template <typename S, int COLL, bool REPORT, bool ODD>
-cudaError_t launch_variant(const Ctx &c, const StepArgs<S> &a, cudaStream_t st) {
-  const dim3 block(BX, BY);
-  const dim3 grid(c.gx, c.gy, c.cfg.nz);
+int stream_grid(const Ctx &c) {
+  constexpr int MAXDEV = 64;
+  static int per_sm[MAXDEV] = {};
+  const int dev = c.cfg.device < MAXDEV ? c.cfg.device : 0;
+  if (per_sm[dev] == 0) {
+    auto kern = stream_kernel<S, COLL, REPORT, ODD>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Layout<S>::BYTES);
+    int nb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, SW, Layout<S>::BYTES);
+    per_sm[dev] = nb > 0 ? nb : 1;
+  }
+  const long long g = (long long)per_sm[dev] * c.num_sms;
+  return (int)(g < c.nseg ? g : c.nseg);
+}
+
+template <typename S, int COLL, bool REPORT, bool ODD>
+cudaError_t launch_variant(const Ctx &c, const StepArgs<S> &a, cudaStream_t st, int64_t *rows) {
   cudaEvent_t *ev = c.ev && c.ev_used < c.ev_cap ? c.ev + 3 * c.ev_used : nullptr;
   if (ev) cudaEventRecord(ev[0], st);
-  bulk_kernel<S, COLL, REPORT, ODD><<<grid, block, 0, st>>>(a);
-  if (ev) cudaEventRecord(ev[1], st);
-  if (c.nspecial > 0) generic_kernel<S, COLL, REPORT, ODD><<<c.nspecial, block, 0, st>>>(a);
+  if (c.use_stream) {
+    StreamArgs<S> sa;
+    sa.a = a;
+    sa.nseg_x = c.nseg_x;
+    sa.nseg = c.nseg;
+    sa.seg_mask = c.seg_mask;
+    sa.masks = c.masks;
+    sa.error = c.error;
+    const int grid = stream_grid<S, COLL, REPORT, ODD>(c);
+    stream_kernel<S, COLL, REPORT, ODD><<<grid, SW, Layout<S>::BYTES, st>>>(sa);
+    *rows = grid;
+    if (ev) cudaEventRecord(ev[1], st);
+  } else {
+    const dim3 block(BX, BY);
+    const dim3 grid(c.gx, c.gy, c.cfg.nz);
+    bulk_kernel<S, COLL, REPORT, ODD><<<grid, block, 0, st>>>(a);
+    if (ev) cudaEventRecord(ev[1], st);
+    if (c.nspecial > 0) generic_kernel<S, COLL, REPORT, ODD><<<c.nspecial, block, 0, st>>>(a);
+    *rows = c.nblocks;
+  }
   if (ev) cudaEventRecord(ev[2], st);
   return cudaGetLastError();
 }
 
 template <typename S, int COLL>
-cudaError_t launch_coll(const Ctx &c, const StepArgs<S> &a, bool report, cudaStream_t st) {
-  if (report) return c.odd_next ? launch_variant<S, COLL, true, true>(c, a, st)
-                                : launch_variant<S, COLL, true, false>(c, a, st);
-  return c.odd_next ? launch_variant<S, COLL, false, true>(c, a, st)
-                    : launch_variant<S, COLL, false, false>(c, a, st);
+cudaError_t launch_coll(const Ctx &c, const StepArgs<S> &a, bool report, cudaStream_t st, int64_t *rows) {
+  if (report) return c.odd_next ? launch_variant<S, COLL, true, true>(c, a, st, rows)
+                                : launch_variant<S, COLL, true, false>(c, a, st, rows);
+  return c.odd_next ? launch_variant<S, COLL, false, true>(c, a, st, rows)
+                    : launch_variant<S, COLL, false, false>(c, a, st, rows);
 }
 
 template <typename S>
 cudaError_t launch_step(const Ctx &c, bool report, cudaStream_t st) {
   const StepArgs<S> a = make_args<S>(c);
   cudaError_t e;
+  int64_t rows = 0;
   switch (c.cfg.collision) {
-    case LBM_BGK: e = launch_coll<S, COLL_BGK>(c, a, report, st); break;
-    case LBM_TRT: e = launch_coll<S, COLL_TRT>(c, a, report, st); break;
-    default: e = launch_coll<S, COLL_LES>(c, a, report, st); break;
+    case LBM_BGK: e = launch_coll<S, COLL_BGK>(c, a, report, st, &rows); break;
+    case LBM_TRT: e = launch_coll<S, COLL_TRT>(c, a, report, st, &rows); break;
+    default: e = launch_coll<S, COLL_LES>(c, a, report, st, &rows); break;
   }
   if (e != cudaSuccess) return e;
-  return report ? launch_finalize(c, st) : cudaSuccess;
+  return report ? launch_finalize(c, rows, st) : cudaSuccess;
+}
+
+template <typename S>
+cudaError_t launch_link_masks(const Ctx &c, cudaStream_t st) {
+  if (c.nmasked == 0) return cudaSuccess;
+  link_mask_kernel<S><<<c.nmasked, SW, 0, st>>>(make_args<S>(c), c.nseg_x, c.seg_list, c.nmasked, c.masks);
+  return cudaGetLastError();
 }
 
 template <typename S>
@@ -114,6 +155,7 @@ cudaError_t launch_export(const Ctx &c, void *dst, int dtype, cudaStream_t st) {
   template cudaError_t launch_init<S>(const Ctx &, double, cudaStream_t);                     \
   template cudaError_t launch_init_random<S>(const Ctx &, double, double, uint64_t, cudaStream_t); \
   template cudaError_t launch_import<S>(const Ctx &, const void *, int, cudaStream_t);        \
-  template cudaError_t launch_export<S>(const Ctx &, void *, int, cudaStream_t);
+  template cudaError_t launch_export<S>(const Ctx &, void *, int, cudaStream_t);                \
+  template cudaError_t launch_link_masks<S>(const Ctx &, cudaStream_t);
 
 }  // namespace lbmh

@@ -1,0 +1,459 @@
+// lbm_stream.cuh - the bulk-copy (TMA) fed AA step: the main sm_103a kernel.
+//
+// The lattice is cut into row segments: SW consecutive cells of one x-row
+// (y, z). A persistent CTA of SW threads walks its share of segments. For each
+// segment one thread issues, per population slot, a cp.async.bulk copy of the
+// contiguous row piece the segment's cells read (with a 16-byte halo on the
+// side a +-x shift needs) into shared memory; an mbarrier counts the bytes.
+// The cells are then updated in place in shared memory: in the AA scheme the
+// post-collision population p of a cell goes exactly where the input of
+// population opp(p) of the same cell came from, so each thread only touches
+// its own elements. The same row pieces are then bulk-stored back to HBM.
+// Three stages keep two segments' copies in flight while one is computed;
+// the copies occupy no registers, so the bytes in flight per SM do not depend
+// on occupancy.
+//
+// Only the elements a segment owns are written back: on an odd step the row
+// pieces of x-shifted slots are offset by one cell, so their aligned middle
+// goes back by bulk copy and the few ragged edge elements by plain stores.
+// Halo elements that belong to a neighbouring segment are read but never used.
+//
+// Walls: free-slip rows and the lid row only change which row and slot a
+// population's piece comes from (and, for the lid, adds the moving-wall term),
+// uniformly for the whole segment. Segments within reach of the obstacle carry
+// a per-cell link mask (bit q: population q bounces back, bit 19: obstacle
+// cell); a bounce-back input is fetched with one plain load from where the
+// cell parked it on the previous step (lbm_device.cuh explains the parking).
+#pragma once
+
+#include "lbm_device.cuh"
+
+namespace lbmk {
+
+constexpr int SW = 256;  // cells per segment = threads per CTA
+constexpr int NST = 3;   // pipeline stages
+constexpr uint32_t MASK_SOLID = 1u << 19;
+constexpr long long WAIT_LIMIT = 1ll << 26;  // mbarrier polls before a step gives up
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+__device__ __forceinline__ void bulk_store(void *dst, const void *src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_addr(src)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read_1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// ---------------------------------------------------------------------------
+// compensated float32 sums (Knuth's TwoSum): a float pair carries ~44 bits,
+// so the warp and segment sums of the report fields lose nothing a float64
+// sum would keep; float64 is used only across warps and CTAs.
+
+struct CSum {
+  float hi, lo;
+};
+__device__ __forceinline__ CSum csum_add(CSum a, CSum b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bp = __fsub_rn(s, a.hi);
+  const float ap = __fsub_rn(s, bp);
+  const float e = __fadd_rn(__fsub_rn(a.hi, ap), __fsub_rn(b.hi, bp));
+  const float lo = __fadd_rn(__fadd_rn(a.lo, b.lo), e);
+  const float hi = __fadd_rn(s, lo);
+  return {hi, __fsub_rn(lo, __fsub_rn(hi, s))};
+}
+__device__ __forceinline__ CSum warp_csum(float v) {
+  CSum x{v, 0.f};
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    CSum y{__shfl_down_sync(0xffffffffu, x.hi, o), __shfl_down_sync(0xffffffffu, x.lo, o)};
+    x = csum_add(x, y);
+  }
+  return x;
+}
+
+template <typename S>
+struct StreamArgs {
+  StepArgs<S> a;
+  int nseg_x;               // segments per x-row
+  int nseg;                 // segments in the lattice
+  const int *seg_mask;      // per segment: first mask word, or -1 (no obstacle within reach)
+  const uint32_t *masks;    // link masks, SW words per masked segment
+  unsigned int *error;      // nonzero after a wait gave up
+};
+
+template <typename S>
+struct Seg {
+  int y, z, x0, w;
+};
+
+template <typename S>
+__device__ __forceinline__ Seg<S> decode_seg(const StreamArgs<S> &sa, int seg) {
+  Seg<S> g;
+  const int sx = seg % sa.nseg_x;
+  const int row = seg / sa.nseg_x;
+  g.y = row % sa.a.ny;
+  g.z = row / sa.a.ny;
+  g.x0 = sx * SW;
+  g.w = min(SW, sa.a.nx - g.x0);
+  return g;
+}
+
+// Where population q's row piece lives for a segment: slot, row, x-shift.
+struct Piece {
+  int slot, ys, zs, shift;
+};
+
+template <int q, bool ODD, typename S>
+__device__ __forceinline__ Piece piece(const StepArgs<S> &a, int y, int z) {
+  Piece p;
+  if (!ODD) {
+    p.slot = q;
+    p.ys = y;
+    p.zs = z;
+    p.shift = 0;
+    return p;
+  }
+  int ys = y - cy(q), zs = z - cz(q);
+  bool ry = false, rz = false, lid = false;
+  if (a.lateral == SIDE_PERIODIC) {
+    ys += ys < 0 ? a.ny : 0;
+    ys -= ys >= a.ny ? a.ny : 0;
+  } else {
+    const bool lo = ys < 0, hi = ys >= a.ny;
+    lid = hi && a.lateral == SIDE_LID;
+    ry = lo || (hi && a.lateral == SIDE_SLIP);
+    ys = (ry || lid) ? y : ys;
+  }
+  if (a.vertical == SIDE_PERIODIC) {
+    zs += zs < 0 ? a.nz : 0;
+    zs -= zs >= a.nz ? a.nz : 0;
+  } else {
+    rz = zs < 0 || zs >= a.nz;
+    zs = rz ? z : zs;
+  }
+  if (lid) {
+    // the lid bounces population q back into the cell itself: its own slot q
+    p.slot = q;
+    p.ys = y;
+    p.zs = z;
+    p.shift = 0;
+    return p;
+  }
+  constexpr int s00 = opp(q);
+  constexpr int s01 = opp(dir(cx(q), cy(q), -cz(q)));
+  constexpr int s10 = opp(dir(cx(q), -cy(q), cz(q)));
+  constexpr int s11 = opp(dir(cx(q), -cy(q), -cz(q)));
+  p.slot = ry ? (rz ? s11 : s10) : (rz ? s01 : s00);
+  p.ys = ys;
+  p.zs = zs;
+  p.shift = -cx(q);
+  return p;
+}
+
+template <typename S>
+struct Layout {
+  static constexpr int H = 16 / (int)sizeof(S);        // halo: one 16-byte vector
+  static constexpr int BUF = SW + 2 * H;               // elements per row-piece buffer
+  static constexpr int STAGE = Q * BUF;                // elements per stage
+  static constexpr size_t BYTES = (size_t)NST * STAGE * sizeof(S) + NST * sizeof(uint64_t);
+};
+
+// Issue the copies of one segment into one stage (one thread).
+template <typename S, bool ODD>
+__device__ __forceinline__ void issue_loads(const StreamArgs<S> &sa, int seg, S *stage, uint64_t *bar) {
+  using L = Layout<S>;
+  const StepArgs<S> &a = sa.a;
+  const Seg<S> g = decode_seg(sa, seg);
+  uint32_t bytes = 0;
+  static_for<Q>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    const Piece p = piece<q, ODD>(a, g.y, g.z);
+    bytes += (uint32_t)((g.w + (p.shift != 0 ? L::H : 0)) * sizeof(S));
+  });
+  mbar_arrive_expect_tx(bar, bytes);
+  static_for<Q>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    const Piece p = piece<q, ODD>(a, g.y, g.z);
+    const S *row = a.slot[p.slot] + ((size_t)p.zs * a.ny + p.ys) * a.nx;
+    S *buf = stage + q * L::BUF;
+    if (p.shift == 0) {
+      bulk_load(buf + L::H, row + g.x0, g.w * sizeof(S), bar);
+    } else if (p.shift < 0) {
+      // cells read x-1: elements [x0-1, x0+w-1); load [x0-H, x0+w)
+      if (g.x0 == 0) {
+        bulk_load(buf, row + a.nx - L::H, L::H * sizeof(S), bar);
+        bulk_load(buf + L::H, row, g.w * sizeof(S), bar);
+      } else {
+        bulk_load(buf, row + g.x0 - L::H, (g.w + L::H) * sizeof(S), bar);
+      }
+    } else {
+      // cells read x+1: elements [x0+1, x0+w+1); load [x0, x0+w+H)
+      if (g.x0 + g.w == a.nx) {
+        bulk_load(buf + L::H, row + g.x0, g.w * sizeof(S), bar);
+        bulk_load(buf + L::H + g.w, row, L::H * sizeof(S), bar);
+      } else {
+        bulk_load(buf + L::H, row + g.x0, (g.w + L::H) * sizeof(S), bar);
+      }
+    }
+  });
+}
+
+// Bulk-store the aligned middle of every row piece the segment owns (one thread).
+template <typename S, bool ODD>
+__device__ __forceinline__ void issue_stores(const StreamArgs<S> &sa, int seg, S *stage) {
+  using L = Layout<S>;
+  const StepArgs<S> &a = sa.a;
+  const Seg<S> g = decode_seg(sa, seg);
+  static_for<Q>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    const Piece p = piece<q, ODD>(a, g.y, g.z);
+    S *row = a.slot[p.slot] + ((size_t)p.zs * a.ny + p.ys) * a.nx;
+    S *buf = stage + q * L::BUF;
+    if (p.shift == 0) bulk_store(row + g.x0, buf + L::H, g.w * sizeof(S));
+    else if (p.shift < 0) bulk_store(row + g.x0, buf + L::H, (g.w - L::H) * sizeof(S));
+    else bulk_store(row + g.x0 + L::H, buf + 2 * L::H, (g.w - L::H) * sizeof(S));
+  });
+  bulk_commit();
+}
+
+// The ragged edge elements of x-shifted pieces: thread t < Q*H stores one.
+template <typename S, bool ODD>
+__device__ __forceinline__ void edge_stores(const StreamArgs<S> &sa, int seg, const S *stage, int t) {
+  using L = Layout<S>;
+  if (!ODD || t >= Q * L::H) return;
+  const StepArgs<S> &a = sa.a;
+  const Seg<S> g = decode_seg(sa, seg);
+  const int qi = t / L::H, k = t % L::H;
+  static_for<Q>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    if (q != qi || cx(q) == 0) return;
+    const Piece p = piece<q, ODD>(a, g.y, g.z);
+    if (p.shift == 0) return;
+    S *row = a.slot[p.slot] + ((size_t)p.zs * a.ny + p.ys) * a.nx;
+    const S *buf = stage + q * L::BUF;
+    int e, si;  // element index in the row, index in the buffer
+    if (p.shift < 0) {
+      // owned: {x0-1} and [x0+w-H, x0+w-1)
+      if (k == 0) {
+        e = g.x0 == 0 ? a.nx - 1 : g.x0 - 1;
+        si = L::H - 1;
+      } else {
+        e = g.x0 + g.w - L::H + k - 1;
+        si = g.w + k - 1;
+      }
+    } else {
+      // owned: [x0+1, x0+H) and {x0+w}
+      if (k < L::H - 1) {
+        e = g.x0 + 1 + k;
+        si = L::H + 1 + k;
+      } else {
+        e = g.x0 + g.w == a.nx ? 0 : g.x0 + g.w;
+        si = L::H + g.w;
+      }
+    }
+    row[e] = buf[si];
+  });
+}
+
+// The one-cell update, reading and writing the stage buffers in place.
+template <typename S, int COLL, bool REPORT, bool ODD>
+__device__ __forceinline__ void stream_cell(const StreamArgs<S> &sa, const Seg<S> &g, S *stage, int i,
+                                            bool lid_row, uint32_t m, float v[NSUM]) {
+  using T = typename Store<S>::T;
+  using L = Layout<S>;
+  const StepArgs<S> &a = sa.a;
+  const bool here = (m & MASK_SOLID) != 0;
+  if (here && !REPORT) return;
+  const int x = g.x0 + i;
+  const int idx = (g.z * a.ny + g.y) * a.nx + x;
+  // buffer element of population q for this cell (the lid row's y-bounced pieces are unshifted)
+  auto pos = [&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    if (!ODD || cx(q) == 0) return q * L::BUF + L::H + i;
+    if (cy(q) == -1 && lid_row) return q * L::BUF + L::H + i;
+    return q * L::BUF + L::H + i - cx(q);
+  };
+  T d[Q];
+  float mx = 0.f, my = 0.f, mz = 0.f;
+  static_for<Q>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    const bool bounce = (m >> q) & 1u;
+    T val;
+    if (!bounce) {
+      val = Store<S>::template load<q>(stage + pos(qc));
+    } else {
+      const Link<S> k = make_link<S, q>(a, x, g.y, g.z);
+      const T wall_term = T(6) * T(wq(q)) * k.cu;
+      if (here) {
+        val = wall_term;
+      } else {
+        // parked on the previous step: own slot q (odd step) or the obstacle cell's slot (even)
+        const T got = Store<S>::template load<q>(ODD ? a.slot[q] + idx : k.L);
+        val = got + wall_term;
+        const float hit = (float)(T(2) * (got + T(wq(q))) + wall_term);
+        mx += hit * (float)(-cx(q));
+        my += hit * (float)(-cy(q));
+        mz += hit * (float)(-cz(q));
+      }
+    }
+    if (cy(q) == -1 && lid_row) {
+      // moving lid above the top row: the cell's own population comes back with the wall term
+      const T lid_term = T(6) * T(wq(q)) * (T(cx(q)) * a.u_lid);
+      val = here ? lid_term : val + lid_term;
+    }
+    d[q] = val;
+  });
+  const Moments<T> mo = moments<T>(d, !here);
+  if (!here) {
+    collide<T, COLL>(d, mo, a.omega_bgk, a.tau0, a.smag_c, a.magic);
+    const T t = fmax(T(0), (T(x) - a.sponge_start) * a.inv_sponge_len);
+    const T sigma = a.sponge_strength * t * t;
+    if (sigma != T(0)) sponge<T>(d, mo, sigma, a.u0);
+    static_for<Q>([&](auto pc) {
+      constexpr int p = decltype(pc)::value;
+      // output p goes where input opp(p) came from
+      Store<S>::template store<p>(stage + pos(std::integral_constant<int, opp(p)>{}), d[p]);
+    });
+  }
+  if (REPORT) diagnostics<T>(a.fld, idx, mo, mx, my, mz, v);
+}
+
+template <typename S, int COLL, bool REPORT, bool ODD>
+__global__ void __launch_bounds__(SW) stream_kernel(const __grid_constant__ StreamArgs<S> sa) {
+  using L = Layout<S>;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  S *stages = reinterpret_cast<S *>(smem_raw);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + (size_t)NST * L::STAGE * sizeof(S));
+  __shared__ double red[SW / 32][NSUM];
+  const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  // this CTA's segments: blockIdx.x, blockIdx.x + gridDim.x, ...
+  const int first = blockIdx.x, stride = gridDim.x;
+  const int count = first < sa.nseg ? (sa.nseg - 1 - first) / stride + 1 : 0;
+  if (tid == 0) {
+    for (int s = 0; s < NST; ++s) mbar_init(&bars[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    fence_async_smem();
+    for (int k = 0; k < NST - 1 && k < count; ++k)
+      issue_loads<S, ODD>(sa, first + k * stride, stages + k * L::STAGE, &bars[k]);
+  }
+  __syncthreads();
+  CSum acc[NSUM];
+#pragma unroll
+  for (int k = 0; k < NSUM; ++k) acc[k] = {0.f, 0.f};
+  int it = 0;
+  for (; it < count; ++it) {
+    const int seg = first + it * stride;
+    const int st = it % NST;
+    S *stage = stages + st * L::STAGE;
+    // wait for the segment's bytes (bounded: a lost copy must not hang the GPU)
+    long long polls = 0;
+    bool ok = true;
+    while (!mbar_try_wait(&bars[st], (uint32_t)((it / NST) & 1))) {
+      if (++polls > WAIT_LIMIT) {
+        ok = false;
+        break;
+      }
+    }
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) {
+        atomicOr(sa.error, 1u);
+        // let the copies already issued land before the CTA leaves (bounded again)
+        for (int k = it; k < count && k < it + NST - 1; ++k) {
+          long long p2 = 0;
+          while (!mbar_try_wait(&bars[k % NST], (uint32_t)((k / NST) & 1)) && ++p2 < WAIT_LIMIT) {
+          }
+        }
+      }
+      break;
+    }
+    const Seg<S> g = decode_seg(sa, seg);
+    const int mslot = sa.seg_mask[seg];
+    const bool lid_row = sa.a.lateral == SIDE_LID && g.y == sa.a.ny - 1;
+    float v[NSUM] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (tid < g.w) {
+      const uint32_t m = mslot >= 0 ? sa.masks[mslot + tid] : 0u;
+      stream_cell<S, COLL, REPORT, ODD>(sa, g, stage, tid, lid_row, m, v);
+    }
+    if (REPORT) {
+#pragma unroll
+      for (int k = 0; k < NSUM; ++k) {
+        const CSum w = warp_csum(v[k]);
+        if (lane == 0) acc[k] = csum_add(acc[k], w);
+      }
+    }
+    __syncthreads();
+    if (tid == 0) {
+      fence_async_smem();
+      issue_stores<S, ODD>(sa, seg, stage);
+      const int nxt = it + NST - 1;
+      if (nxt < count) {
+        // the stage the next loads go to was stored from on the previous iteration
+        bulk_wait_read_1();
+        issue_loads<S, ODD>(sa, first + nxt * stride, stages + (nxt % NST) * L::STAGE, &bars[nxt % NST]);
+      }
+    }
+    edge_stores<S, ODD>(sa, seg, stage, tid);
+  }
+  if (tid == 0) bulk_wait_all();
+  if (REPORT) {
+    if (lane == 0)
+      for (int k = 0; k < NSUM; ++k) red[warp][k] = (double)acc[k].hi + (double)acc[k].lo;
+    __syncthreads();
+    if (tid < NSUM) {
+      double s = 0.0;
+      for (int w = 0; w < SW / 32; ++w) s += red[w][tid];
+      sa.a.partials[(size_t)blockIdx.x * NSUM + tid] = s;
+    }
+  }
+}
+
+// Link masks of the masked segments: bit q when population q of the cell
+// streams from an obstacle cell (bounce-back), MASK_SOLID for an obstacle cell.
+template <typename S>
+__global__ void link_mask_kernel(const __grid_constant__ StepArgs<S> a, int nseg_x, const int *seg_list,
+                                 int nlist, uint32_t *masks) {
+  const int k = blockIdx.x;
+  if (k >= nlist) return;
+  const int seg = seg_list[k];
+  const int sx = seg % nseg_x, row = seg / nseg_x;
+  const int y = row % a.ny, z = row / a.ny;
+  const int i = threadIdx.x, x = sx * SW + i;
+  uint32_t m = 0;
+  if (x < a.nx) {
+    if (solid(a.geo, x, y, z)) m |= MASK_SOLID;
+    static_for<Q>([&](auto qc) {
+      constexpr int q = decltype(qc)::value;
+      if (make_link<S, q>(a, x, y, z).wall) m |= 1u << q;
+    });
+  }
+  masks[(size_t)k * SW + i] = m;
+}
+
+}  // namespace lbmk

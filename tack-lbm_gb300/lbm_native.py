@@ -17,6 +17,7 @@ NO_OBSTACLE, CYLINDER, SPHERE, BOX = 0, 1, 2, 3
 PERIODIC, SLIP, LID = 0, 1, 2
 F32, F16, BF16, F64 = 0, 1, 2, 3
 HOST, DEVICE = 0, 1
+FLAG_SIMT = 1
 FIELDS = ("ux", "uy", "uz", "p", "vmag", "r_rho", "r_ux", "r_uy", "r_uz", "r_ke", "fx", "fy", "fz")
 MONITORS = ("continuity", "momentum_x", "momentum_y", "momentum_z", "energy", "drag", "lift")
 STORAGE = {"f32": F32, "f16": F16, "bf16": BF16, "f64": F64}
@@ -45,7 +46,7 @@ class Config(ctypes.Structure):
         ("r", ctypes.c_double), ("hx", ctypes.c_double), ("hy", ctypes.c_double), ("hz", ctypes.c_double),
         ("u0", ctypes.c_double), ("sponge_start", ctypes.c_double), ("sponge_strength", ctypes.c_double),
         ("u_lid", ctypes.c_double), ("omega_rot", ctypes.c_double),
-        ("device", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("device", ctypes.c_int32), ("flags", ctypes.c_int32),
     ]
 
 
