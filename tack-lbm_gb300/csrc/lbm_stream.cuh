@@ -33,7 +33,7 @@ namespace lbmk {
 constexpr int SW = 256;  // cells per segment = threads per CTA
 constexpr int NST = 3;   // pipeline stages
 constexpr uint32_t MASK_SOLID = 1u << 19;
-constexpr long long WAIT_LIMIT = 1ll << 26;  // mbarrier polls before a step gives up
+constexpr long long WAIT_LIMIT = 1ll << 22;  // mbarrier polls before a step gives up
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
