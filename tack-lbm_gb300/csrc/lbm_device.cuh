@@ -104,6 +104,7 @@ struct StepArgs {
   P u_lid;
   P u0, sponge_start, sponge_strength, inv_sponge_len;
   P omega_rot;
+  P wall_ox, wall_oy, wall_inv_r;     // cylinder axis and 1/r for the moving-wall term
   P omega_bgk, tau0, smag_c, magic;   // smag_c = 25.456 cs^2 (lbm.py:93)
   float *fld[13];
   double *partials;       // NSUM doubles per block (report steps)
@@ -521,8 +522,8 @@ __device__ __forceinline__ Link<S> make_link(const StepArgs<S> &a, int x, int y,
   } else if (a.geo.kind == OBS_CYL) {
     const T xm = T(x) - T(0.5) * T(cx(q));
     const T ym = T(y) - T(0.5) * T(cy(q));
-    const T vx = a.omega_rot * (-(ym - T(a.geo.oy)) * T(a.geo.inv_r));
-    const T vy = a.omega_rot * ((xm - T(a.geo.ox)) * T(a.geo.inv_r));
+    const T vx = a.omega_rot * (-(ym - a.wall_oy) * a.wall_inv_r);
+    const T vy = a.omega_rot * ((xm - a.wall_ox) * a.wall_inv_r);
     cu = T(cx(q)) * vx + T(cy(q)) * vy;
   }
   k.cu = cu;

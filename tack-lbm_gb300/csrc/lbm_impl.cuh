@@ -29,6 +29,9 @@ StepArgs<S> make_args(const Ctx &c) {
   a.sponge_strength = (P)g.sponge_strength;
   a.inv_sponge_len = (P)(1.0 / ((double)g.nx - g.sponge_start));
   a.omega_rot = (P)c.omega_rot;
+  a.wall_ox = (P)g.ox;
+  a.wall_oy = (P)g.oy;
+  a.wall_inv_r = g.r != 0.0 ? (P)(1.0 / g.r) : (P)0;
   a.omega_bgk = (P)(1.0 / (3.0 * g.nu + 0.5));
   a.tau0 = (P)(3.0 * g.nu + 0.5);
   a.smag_c = (P)(25.456 * g.cs * g.cs);

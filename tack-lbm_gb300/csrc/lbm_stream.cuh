@@ -107,21 +107,45 @@ struct StreamArgs {
   unsigned int *error;      // nonzero after a wait gave up
 };
 
-template <typename S>
-struct Seg {
-  int y, z, x0, w;
+// One segment: row (y, z), cells [x0, x0 + w), first link-mask word (or -1).
+struct SegInfo {
+  int y, z, x0, w, mslot;
 };
 
 template <typename S>
-__device__ __forceinline__ Seg<S> decode_seg(const StreamArgs<S> &sa, int seg) {
-  Seg<S> g;
+__device__ __forceinline__ SegInfo decode_seg(const StreamArgs<S> &sa, int seg) {
+  SegInfo g;
   const int sx = seg % sa.nseg_x;
   const int row = seg / sa.nseg_x;
   g.y = row % sa.a.ny;
   g.z = row / sa.a.ny;
   g.x0 = sx * SW;
   g.w = min(SW, sa.a.nx - g.x0);
+  g.mslot = sa.seg_mask[seg];
   return g;
+}
+
+// Direction table for lane-parallel copy issue: lane q handles population q.
+struct DirTab {
+  signed char cx, cy, cz, s00, s01, s10, s11, pad;
+};
+
+__device__ __forceinline__ void fill_dirtab(DirTab *tab, int tid) {
+  static_for<Q>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    if (tid == q) {
+      DirTab t;
+      t.cx = (signed char)cx(q);
+      t.cy = (signed char)cy(q);
+      t.cz = (signed char)cz(q);
+      t.s00 = (signed char)opp(q);
+      t.s01 = (signed char)opp(dir(cx(q), cy(q), -cz(q)));
+      t.s10 = (signed char)opp(dir(cx(q), -cy(q), cz(q)));
+      t.s11 = (signed char)opp(dir(cx(q), -cy(q), -cz(q)));
+      t.pad = 0;
+      tab[q] = t;
+    }
+  });
 }
 
 // Where population q's row piece lives for a segment: slot, row, x-shift.
@@ -129,17 +153,15 @@ struct Piece {
   int slot, ys, zs, shift;
 };
 
-template <int q, bool ODD, typename S>
-__device__ __forceinline__ Piece piece(const StepArgs<S> &a, int y, int z) {
+template <bool ODD, typename S>
+__device__ __forceinline__ Piece piece(const StepArgs<S> &a, const DirTab &t, int q, int y, int z) {
   Piece p;
-  if (!ODD) {
-    p.slot = q;
-    p.ys = y;
-    p.zs = z;
-    p.shift = 0;
-    return p;
-  }
-  int ys = y - cy(q), zs = z - cz(q);
+  p.slot = q;
+  p.ys = y;
+  p.zs = z;
+  p.shift = 0;
+  if (!ODD) return p;
+  int ys = y - t.cy, zs = z - t.cz;
   bool ry = false, rz = false, lid = false;
   if (a.lateral == SIDE_PERIODIC) {
     ys += ys < 0 ? a.ny : 0;
@@ -157,22 +179,12 @@ __device__ __forceinline__ Piece piece(const StepArgs<S> &a, int y, int z) {
     rz = zs < 0 || zs >= a.nz;
     zs = rz ? z : zs;
   }
-  if (lid) {
-    // the lid bounces population q back into the cell itself: its own slot q
-    p.slot = q;
-    p.ys = y;
-    p.zs = z;
-    p.shift = 0;
-    return p;
-  }
-  constexpr int s00 = opp(q);
-  constexpr int s01 = opp(dir(cx(q), cy(q), -cz(q)));
-  constexpr int s10 = opp(dir(cx(q), -cy(q), cz(q)));
-  constexpr int s11 = opp(dir(cx(q), -cy(q), -cz(q)));
-  p.slot = ry ? (rz ? s11 : s10) : (rz ? s01 : s00);
+  // the lid bounces population q back into the cell itself: its own slot q, unshifted
+  if (lid) return p;
+  p.slot = ry ? (rz ? t.s11 : t.s10) : (rz ? t.s01 : t.s00);
   p.ys = ys;
   p.zs = zs;
-  p.shift = -cx(q);
+  p.shift = -t.cx;
   return p;
 }
 
@@ -184,110 +196,107 @@ struct Layout {
   static constexpr size_t BYTES = (size_t)NST * STAGE * sizeof(S) + NST * sizeof(uint64_t);
 };
 
-// Issue the copies of one segment into one stage (one thread).
+// Warp 0 issues one segment's copies into one stage: lane q copies population
+// q's row piece (one or two bulk copies). Each lane first waits until its own
+// bulk stores from this stage (two segments ago) have read the buffer.
 template <typename S, bool ODD>
-__device__ __forceinline__ void issue_loads(const StreamArgs<S> &sa, int seg, S *stage, uint64_t *bar) {
+__device__ __forceinline__ void issue_loads(const StreamArgs<S> &sa, const DirTab *tab, int seg, S *stage,
+                                            uint64_t *bar, SegInfo *info, int lane) {
   using L = Layout<S>;
   const StepArgs<S> &a = sa.a;
-  const Seg<S> g = decode_seg(sa, seg);
+  const SegInfo g = decode_seg(sa, seg);
+  if (lane == 0) *info = g;
+  Piece p{0, 0, 0, 0};
   uint32_t bytes = 0;
-  static_for<Q>([&](auto qc) {
-    constexpr int q = decltype(qc)::value;
-    const Piece p = piece<q, ODD>(a, g.y, g.z);
-    bytes += (uint32_t)((g.w + (p.shift != 0 ? L::H : 0)) * sizeof(S));
-  });
-  mbar_arrive_expect_tx(bar, bytes);
-  static_for<Q>([&](auto qc) {
-    constexpr int q = decltype(qc)::value;
-    const Piece p = piece<q, ODD>(a, g.y, g.z);
-    const S *row = a.slot[p.slot] + ((size_t)p.zs * a.ny + p.ys) * a.nx;
-    S *buf = stage + q * L::BUF;
-    if (p.shift == 0) {
-      bulk_load(buf + L::H, row + g.x0, g.w * sizeof(S), bar);
-    } else if (p.shift < 0) {
-      // cells read x-1: elements [x0-1, x0+w-1); load [x0-H, x0+w)
-      if (g.x0 == 0) {
-        bulk_load(buf, row + a.nx - L::H, L::H * sizeof(S), bar);
-        bulk_load(buf + L::H, row, g.w * sizeof(S), bar);
-      } else {
-        bulk_load(buf, row + g.x0 - L::H, (g.w + L::H) * sizeof(S), bar);
-      }
+  if (lane < Q) {
+    p = piece<ODD>(a, tab[lane], lane, g.y, g.z);
+    bytes = (uint32_t)((g.w + (p.shift != 0 ? L::H : 0)) * sizeof(S));
+  }
+  const uint32_t total = __reduce_add_sync(0xffffffffu, bytes);
+  bulk_wait_read_1();
+  if (lane == 0) mbar_arrive_expect_tx(bar, total);
+  __syncwarp();
+  if (lane >= Q) return;
+  const S *row = a.slot[p.slot] + ((size_t)p.zs * a.ny + p.ys) * a.nx;
+  S *buf = stage + lane * L::BUF;
+  if (p.shift == 0) {
+    bulk_load(buf + L::H, row + g.x0, g.w * sizeof(S), bar);
+  } else if (p.shift < 0) {
+    // cells read x-1: elements [x0-1, x0+w-1); load [x0-H, x0+w)
+    if (g.x0 == 0) {
+      bulk_load(buf, row + a.nx - L::H, L::H * sizeof(S), bar);
+      bulk_load(buf + L::H, row, g.w * sizeof(S), bar);
     } else {
-      // cells read x+1: elements [x0+1, x0+w+1); load [x0, x0+w+H)
-      if (g.x0 + g.w == a.nx) {
-        bulk_load(buf + L::H, row + g.x0, g.w * sizeof(S), bar);
-        bulk_load(buf + L::H + g.w, row, L::H * sizeof(S), bar);
-      } else {
-        bulk_load(buf + L::H, row + g.x0, (g.w + L::H) * sizeof(S), bar);
-      }
+      bulk_load(buf, row + g.x0 - L::H, (g.w + L::H) * sizeof(S), bar);
     }
-  });
+  } else {
+    // cells read x+1: elements [x0+1, x0+w+1); load [x0, x0+w+H)
+    if (g.x0 + g.w == a.nx) {
+      bulk_load(buf + L::H, row + g.x0, g.w * sizeof(S), bar);
+      bulk_load(buf + L::H + g.w, row, L::H * sizeof(S), bar);
+    } else {
+      bulk_load(buf + L::H, row + g.x0, (g.w + L::H) * sizeof(S), bar);
+    }
+  }
 }
 
-// Bulk-store the aligned middle of every row piece the segment owns (one thread).
+// Warp 0 bulk-stores the aligned middle of every row piece the segment owns.
 template <typename S, bool ODD>
-__device__ __forceinline__ void issue_stores(const StreamArgs<S> &sa, int seg, S *stage) {
+__device__ __forceinline__ void issue_stores(const StreamArgs<S> &sa, const DirTab *tab, const SegInfo &g,
+                                             S *stage, int lane) {
   using L = Layout<S>;
+  if (lane >= Q) return;
   const StepArgs<S> &a = sa.a;
-  const Seg<S> g = decode_seg(sa, seg);
-  static_for<Q>([&](auto qc) {
-    constexpr int q = decltype(qc)::value;
-    const Piece p = piece<q, ODD>(a, g.y, g.z);
-    S *row = a.slot[p.slot] + ((size_t)p.zs * a.ny + p.ys) * a.nx;
-    S *buf = stage + q * L::BUF;
-    if (p.shift == 0) bulk_store(row + g.x0, buf + L::H, g.w * sizeof(S));
-    else if (p.shift < 0) bulk_store(row + g.x0, buf + L::H, (g.w - L::H) * sizeof(S));
-    else bulk_store(row + g.x0 + L::H, buf + 2 * L::H, (g.w - L::H) * sizeof(S));
-  });
+  const Piece p = piece<ODD>(a, tab[lane], lane, g.y, g.z);
+  S *row = a.slot[p.slot] + ((size_t)p.zs * a.ny + p.ys) * a.nx;
+  S *buf = stage + lane * L::BUF;
+  if (p.shift == 0) bulk_store(row + g.x0, buf + L::H, g.w * sizeof(S));
+  else if (p.shift < 0) bulk_store(row + g.x0, buf + L::H, (g.w - L::H) * sizeof(S));
+  else bulk_store(row + g.x0 + L::H, buf + 2 * L::H, (g.w - L::H) * sizeof(S));
   bulk_commit();
 }
 
 // The ragged edge elements of x-shifted pieces: thread t < Q*H stores one.
 template <typename S, bool ODD>
-__device__ __forceinline__ void edge_stores(const StreamArgs<S> &sa, int seg, const S *stage, int t) {
+__device__ __forceinline__ void edge_stores(const StreamArgs<S> &sa, const DirTab *tab, const SegInfo &g,
+                                            const S *stage, int t) {
   using L = Layout<S>;
   if (!ODD || t >= Q * L::H) return;
   const StepArgs<S> &a = sa.a;
-  const Seg<S> g = decode_seg(sa, seg);
-  const int qi = t / L::H, k = t % L::H;
-  static_for<Q>([&](auto qc) {
-    constexpr int q = decltype(qc)::value;
-    if (q != qi || cx(q) == 0) return;
-    const Piece p = piece<q, ODD>(a, g.y, g.z);
-    if (p.shift == 0) return;
-    S *row = a.slot[p.slot] + ((size_t)p.zs * a.ny + p.ys) * a.nx;
-    const S *buf = stage + q * L::BUF;
-    int e, si;  // element index in the row, index in the buffer
-    if (p.shift < 0) {
-      // owned: {x0-1} and [x0+w-H, x0+w-1)
-      if (k == 0) {
-        e = g.x0 == 0 ? a.nx - 1 : g.x0 - 1;
-        si = L::H - 1;
-      } else {
-        e = g.x0 + g.w - L::H + k - 1;
-        si = g.w + k - 1;
-      }
+  const int q = t / L::H, k = t % L::H;
+  const Piece p = piece<ODD>(a, tab[q], q, g.y, g.z);
+  if (p.shift == 0) return;
+  S *row = a.slot[p.slot] + ((size_t)p.zs * a.ny + p.ys) * a.nx;
+  const S *buf = stage + q * L::BUF;
+  int e, si;  // element index in the row, index in the buffer
+  if (p.shift < 0) {
+    // owned: {x0-1} and [x0+w-H, x0+w-1)
+    if (k == 0) {
+      e = g.x0 == 0 ? a.nx - 1 : g.x0 - 1;
+      si = L::H - 1;
     } else {
-      // owned: [x0+1, x0+H) and {x0+w}
-      if (k < L::H - 1) {
-        e = g.x0 + 1 + k;
-        si = L::H + 1 + k;
-      } else {
-        e = g.x0 + g.w == a.nx ? 0 : g.x0 + g.w;
-        si = L::H + g.w;
-      }
+      e = g.x0 + g.w - L::H + k - 1;
+      si = g.w + k - 1;
     }
-    row[e] = buf[si];
-  });
+  } else {
+    // owned: [x0+1, x0+H) and {x0+w}
+    if (k < L::H - 1) {
+      e = g.x0 + 1 + k;
+      si = L::H + 1 + k;
+    } else {
+      e = g.x0 + g.w == a.nx ? 0 : g.x0 + g.w;
+      si = L::H + g.w;
+    }
+  }
+  row[e] = buf[si];
 }
 
 // The one-cell update, reading and writing the stage buffers in place.
 template <typename S, int COLL, bool REPORT, bool ODD>
-__device__ __forceinline__ void stream_cell(const StreamArgs<S> &sa, const Seg<S> &g, S *stage, int i,
+__device__ __forceinline__ void stream_cell(const StepArgs<S> &a, const SegInfo &g, S *stage, int i,
                                             bool lid_row, uint32_t m, float v[NSUM]) {
   using T = typename Store<S>::T;
   using L = Layout<S>;
-  const StepArgs<S> &a = sa.a;
   const bool here = (m & MASK_SOLID) != 0;
   if (here && !REPORT) return;
   const int x = g.x0 + i;
@@ -351,25 +360,27 @@ __global__ void __launch_bounds__(SW) stream_kernel(const __grid_constant__ Stre
   S *stages = reinterpret_cast<S *>(smem_raw);
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + (size_t)NST * L::STAGE * sizeof(S));
   __shared__ double red[SW / 32][NSUM];
+  __shared__ DirTab tab[Q];
+  __shared__ SegInfo info[NST];
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
   // this CTA's segments: blockIdx.x, blockIdx.x + gridDim.x, ...
   const int first = blockIdx.x, stride = gridDim.x;
   const int count = first < sa.nseg ? (sa.nseg - 1 - first) / stride + 1 : 0;
+  fill_dirtab(tab, tid);
   if (tid == 0) {
     for (int s = 0; s < NST; ++s) mbar_init(&bars[s], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     fence_async_smem();
-    for (int k = 0; k < NST - 1 && k < count; ++k)
-      issue_loads<S, ODD>(sa, first + k * stride, stages + k * L::STAGE, &bars[k]);
   }
   __syncthreads();
+  if (warp == 0)
+    for (int k = 0; k < NST - 1 && k < count; ++k)
+      issue_loads<S, ODD>(sa, tab, first + k * stride, stages + k * L::STAGE, &bars[k], &info[k], lane);
   CSum acc[NSUM];
 #pragma unroll
   for (int k = 0; k < NSUM; ++k) acc[k] = {0.f, 0.f};
-  int it = 0;
-  for (; it < count; ++it) {
-    const int seg = first + it * stride;
+  for (int it = 0; it < count; ++it) {
     const int st = it % NST;
     S *stage = stages + st * L::STAGE;
     // wait for the segment's bytes (bounded: a lost copy must not hang the GPU)
@@ -393,13 +404,12 @@ __global__ void __launch_bounds__(SW) stream_kernel(const __grid_constant__ Stre
       }
       break;
     }
-    const Seg<S> g = decode_seg(sa, seg);
-    const int mslot = sa.seg_mask[seg];
+    const SegInfo g = info[st];
     const bool lid_row = sa.a.lateral == SIDE_LID && g.y == sa.a.ny - 1;
     float v[NSUM] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (tid < g.w) {
-      const uint32_t m = mslot >= 0 ? sa.masks[mslot + tid] : 0u;
-      stream_cell<S, COLL, REPORT, ODD>(sa, g, stage, tid, lid_row, m, v);
+      const uint32_t m = g.mslot >= 0 ? sa.masks[g.mslot + tid] : 0u;
+      stream_cell<S, COLL, REPORT, ODD>(sa.a, g, stage, tid, lid_row, m, v);
     }
     if (REPORT) {
 #pragma unroll
@@ -408,20 +418,18 @@ __global__ void __launch_bounds__(SW) stream_kernel(const __grid_constant__ Stre
         if (lane == 0) acc[k] = csum_add(acc[k], w);
       }
     }
+    fence_async_smem();  // this thread's shared-memory writes, before the bulk stores read them
     __syncthreads();
-    if (tid == 0) {
-      fence_async_smem();
-      issue_stores<S, ODD>(sa, seg, stage);
+    if (warp == 0) {
+      issue_stores<S, ODD>(sa, tab, g, stage, lane);
       const int nxt = it + NST - 1;
-      if (nxt < count) {
-        // the stage the next loads go to was stored from on the previous iteration
-        bulk_wait_read_1();
-        issue_loads<S, ODD>(sa, first + nxt * stride, stages + (nxt % NST) * L::STAGE, &bars[nxt % NST]);
-      }
+      if (nxt < count)
+        issue_loads<S, ODD>(sa, tab, first + nxt * stride, stages + (nxt % NST) * L::STAGE, &bars[nxt % NST],
+                            &info[nxt % NST], lane);
     }
-    edge_stores<S, ODD>(sa, seg, stage, tid);
+    edge_stores<S, ODD>(sa, tab, g, stage, tid);
   }
-  if (tid == 0) bulk_wait_all();
+  if (warp == 0) bulk_wait_all();
   if (REPORT) {
     if (lane == 0)
       for (int k = 0; k < NSUM; ++k) red[warp][k] = (double)acc[k].hi + (double)acc[k].lo;
