@@ -55,7 +55,7 @@ int stream_grid(const Ctx &c) {
     auto kern = stream_kernel<S, COLL, REPORT, ODD>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Layout<S>::BYTES);
     int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, SW, Layout<S>::BYTES);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, SW + 32, Layout<S>::BYTES);
     per_sm[dev] = nb > 0 ? nb : 1;
   }
   const long long g = (long long)per_sm[dev] * c.num_sms;
@@ -75,7 +75,7 @@ cudaError_t launch_variant(const Ctx &c, const StepArgs<S> &a, cudaStream_t st, 
     sa.masks = c.masks;
     sa.error = c.error;
     const int grid = stream_grid<S, COLL, REPORT, ODD>(c);
-    stream_kernel<S, COLL, REPORT, ODD><<<grid, SW, Layout<S>::BYTES, st>>>(sa);
+    stream_kernel<S, COLL, REPORT, ODD><<<grid, SW + 32, Layout<S>::BYTES, st>>>(sa);
     *rows = grid;
     if (ev) cudaEventRecord(ev[1], st);
   } else {

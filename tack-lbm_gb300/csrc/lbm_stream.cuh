@@ -33,7 +33,7 @@ namespace lbmk {
 constexpr int SW = 256;  // cells per segment = threads per CTA
 constexpr int NST = 3;   // pipeline stages
 constexpr uint32_t MASK_SOLID = 1u << 19;
-constexpr long long WAIT_LIMIT = 1ll << 22;  // mbarrier polls before a step gives up
+constexpr long long WAIT_LIMIT = 1ll << 20;  // mbarrier polls before a step gives up
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -66,7 +66,7 @@ __device__ __forceinline__ void bulk_store(void *dst, const void *src, uint32_t 
                : "memory");
 }
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_read_1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read_0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
@@ -193,15 +193,14 @@ struct Layout {
   static constexpr int H = 16 / (int)sizeof(S);        // halo: one 16-byte vector
   static constexpr int BUF = SW + 2 * H;               // elements per row-piece buffer
   static constexpr int STAGE = Q * BUF;                // elements per stage
-  static constexpr size_t BYTES = (size_t)NST * STAGE * sizeof(S) + NST * sizeof(uint64_t);
+  static constexpr size_t BYTES = (size_t)NST * STAGE * sizeof(S) + 2 * NST * sizeof(uint64_t);
 };
 
-// Warp 0 issues one segment's copies into one stage: lane q copies population
-// q's row piece (one or two bulk copies). Each lane first waits until its own
-// bulk stores from this stage (two segments ago) have read the buffer.
+// The producer warp issues one segment's copies into one stage: lane q copies
+// population q's row piece (one or two bulk copies) and signals `full`.
 template <typename S, bool ODD>
 __device__ __forceinline__ void issue_loads(const StreamArgs<S> &sa, const DirTab *tab, int seg, S *stage,
-                                            uint64_t *bar, SegInfo *info, int lane) {
+                                            uint64_t *full, SegInfo *info, int lane) {
   using L = Layout<S>;
   const StepArgs<S> &a = sa.a;
   const SegInfo g = decode_seg(sa, seg);
@@ -213,34 +212,33 @@ __device__ __forceinline__ void issue_loads(const StreamArgs<S> &sa, const DirTa
     bytes = (uint32_t)((g.w + (p.shift != 0 ? L::H : 0)) * sizeof(S));
   }
   const uint32_t total = __reduce_add_sync(0xffffffffu, bytes);
-  bulk_wait_read_1();
-  if (lane == 0) mbar_arrive_expect_tx(bar, total);
+  if (lane == 0) mbar_arrive_expect_tx(full, total);
   __syncwarp();
   if (lane >= Q) return;
   const S *row = a.slot[p.slot] + ((size_t)p.zs * a.ny + p.ys) * a.nx;
   S *buf = stage + lane * L::BUF;
   if (p.shift == 0) {
-    bulk_load(buf + L::H, row + g.x0, g.w * sizeof(S), bar);
+    bulk_load(buf + L::H, row + g.x0, g.w * sizeof(S), full);
   } else if (p.shift < 0) {
     // cells read x-1: elements [x0-1, x0+w-1); load [x0-H, x0+w)
     if (g.x0 == 0) {
-      bulk_load(buf, row + a.nx - L::H, L::H * sizeof(S), bar);
-      bulk_load(buf + L::H, row, g.w * sizeof(S), bar);
+      bulk_load(buf, row + a.nx - L::H, L::H * sizeof(S), full);
+      bulk_load(buf + L::H, row, g.w * sizeof(S), full);
     } else {
-      bulk_load(buf, row + g.x0 - L::H, (g.w + L::H) * sizeof(S), bar);
+      bulk_load(buf, row + g.x0 - L::H, (g.w + L::H) * sizeof(S), full);
     }
   } else {
     // cells read x+1: elements [x0+1, x0+w+1); load [x0, x0+w+H)
     if (g.x0 + g.w == a.nx) {
-      bulk_load(buf + L::H, row + g.x0, g.w * sizeof(S), bar);
-      bulk_load(buf + L::H + g.w, row, L::H * sizeof(S), bar);
+      bulk_load(buf + L::H, row + g.x0, g.w * sizeof(S), full);
+      bulk_load(buf + L::H + g.w, row, L::H * sizeof(S), full);
     } else {
-      bulk_load(buf + L::H, row + g.x0, (g.w + L::H) * sizeof(S), bar);
+      bulk_load(buf + L::H, row + g.x0, (g.w + L::H) * sizeof(S), full);
     }
   }
 }
 
-// Warp 0 bulk-stores the aligned middle of every row piece the segment owns.
+// The producer warp bulk-stores the aligned middle of every row piece the segment owns.
 template <typename S, bool ODD>
 __device__ __forceinline__ void issue_stores(const StreamArgs<S> &sa, const DirTab *tab, const SegInfo &g,
                                              S *stage, int lane) {
@@ -292,12 +290,13 @@ __device__ __forceinline__ void edge_stores(const StreamArgs<S> &sa, const DirTa
 }
 
 // The one-cell update, reading and writing the stage buffers in place.
-template <typename S, int COLL, bool REPORT, bool ODD>
+// PLAIN: no obstacle cell within reach and not the lid row.
+template <typename S, int COLL, bool REPORT, bool ODD, bool PLAIN>
 __device__ __forceinline__ void stream_cell(const StepArgs<S> &a, const SegInfo &g, S *stage, int i,
                                             bool lid_row, uint32_t m, float v[NSUM]) {
   using T = typename Store<S>::T;
   using L = Layout<S>;
-  const bool here = (m & MASK_SOLID) != 0;
+  const bool here = !PLAIN && (m & MASK_SOLID) != 0;
   if (here && !REPORT) return;
   const int x = g.x0 + i;
   const int idx = (g.z * a.ny + g.y) * a.nx + x;
@@ -305,16 +304,15 @@ __device__ __forceinline__ void stream_cell(const StepArgs<S> &a, const SegInfo 
   auto pos = [&](auto qc) {
     constexpr int q = decltype(qc)::value;
     if (!ODD || cx(q) == 0) return q * L::BUF + L::H + i;
-    if (cy(q) == -1 && lid_row) return q * L::BUF + L::H + i;
+    if (!PLAIN && cy(q) == -1 && lid_row) return q * L::BUF + L::H + i;
     return q * L::BUF + L::H + i - cx(q);
   };
   T d[Q];
   float mx = 0.f, my = 0.f, mz = 0.f;
   static_for<Q>([&](auto qc) {
     constexpr int q = decltype(qc)::value;
-    const bool bounce = (m >> q) & 1u;
     T val;
-    if (!bounce) {
+    if (PLAIN || !((m >> q) & 1u)) {
       val = Store<S>::template load<q>(stage + pos(qc));
     } else {
       const Link<S> k = make_link<S, q>(a, x, g.y, g.z);
@@ -331,7 +329,7 @@ __device__ __forceinline__ void stream_cell(const StepArgs<S> &a, const SegInfo 
         mz += hit * (float)(-cz(q));
       }
     }
-    if (cy(q) == -1 && lid_row) {
+    if (!PLAIN && cy(q) == -1 && lid_row) {
       // moving lid above the top row: the cell's own population comes back with the wall term
       const T lid_term = T(6) * T(wq(q)) * (T(cx(q)) * a.u_lid);
       val = here ? lid_term : val + lid_term;
@@ -353,12 +351,29 @@ __device__ __forceinline__ void stream_cell(const StepArgs<S> &a, const SegInfo 
   if (REPORT) diagnostics<T>(a.fld, idx, mo, mx, my, mz, v);
 }
 
+__device__ __forceinline__ bool wait_phase(uint64_t *bar, uint32_t parity) {
+  long long polls = 0;
+  while (!mbar_try_wait(bar, parity))
+    if (++polls > WAIT_LIMIT) return false;
+  return true;
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void consumer_sync() {
+  asm volatile("bar.sync 1, %0;" ::"n"(SW) : "memory");
+}
+
+// SW consumer threads (one cell each) plus one producer warp that owns the copies.
+// Stage s: `full` completes when the segment's bytes landed, `empty` when all
+// consumers are done with it (their updates fenced for the bulk stores).
 template <typename S, int COLL, bool REPORT, bool ODD>
-__global__ void __launch_bounds__(SW) stream_kernel(const __grid_constant__ StreamArgs<S> sa) {
+__global__ void __launch_bounds__(SW + 32) stream_kernel(const __grid_constant__ StreamArgs<S> sa) {
   using L = Layout<S>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   S *stages = reinterpret_cast<S *>(smem_raw);
-  uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + (size_t)NST * L::STAGE * sizeof(S));
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + (size_t)NST * L::STAGE * sizeof(S));
+  uint64_t *empty = full + NST;
   __shared__ double red[SW / 32][NSUM];
   __shared__ DirTab tab[Q];
   __shared__ SegInfo info[NST];
@@ -369,47 +384,61 @@ __global__ void __launch_bounds__(SW) stream_kernel(const __grid_constant__ Stre
   const int count = first < sa.nseg ? (sa.nseg - 1 - first) / stride + 1 : 0;
   fill_dirtab(tab, tid);
   if (tid == 0) {
-    for (int s = 0; s < NST; ++s) mbar_init(&bars[s], 1);
+    for (int s = 0; s < NST; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], SW);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     fence_async_smem();
   }
   __syncthreads();
-  if (warp == 0)
-    for (int k = 0; k < NST - 1 && k < count; ++k)
-      issue_loads<S, ODD>(sa, tab, first + k * stride, stages + k * L::STAGE, &bars[k], &info[k], lane);
+
+  if (warp == SW / 32) {
+    // producer warp
+    for (int k = 0; k < NST && k < count; ++k)
+      issue_loads<S, ODD>(sa, tab, first + k * stride, stages + k * L::STAGE, &full[k], &info[k], lane);
+    for (int it = 0; it < count; ++it) {
+      const int st = it % NST;
+      if (!__all_sync(0xffffffffu, wait_phase(&empty[st], (uint32_t)((it / NST) & 1)))) {
+        if (lane == 0) atomicOr(sa.error, 1u);
+        break;
+      }
+      issue_stores<S, ODD>(sa, tab, info[st], stages + st * L::STAGE, lane);
+      const int nxt = it + NST;
+      if (nxt < count) {
+        bulk_wait_read_0();  // this lane's stores out of the stage have read it
+        __syncwarp();
+        issue_loads<S, ODD>(sa, tab, first + nxt * stride, stages + st * L::STAGE, &full[st], &info[st], lane);
+      }
+    }
+    bulk_wait_all();
+    return;
+  }
+
+  // consumer warps
   CSum acc[NSUM];
 #pragma unroll
   for (int k = 0; k < NSUM; ++k) acc[k] = {0.f, 0.f};
+  bool bad = false;
   for (int it = 0; it < count; ++it) {
     const int st = it % NST;
     S *stage = stages + st * L::STAGE;
-    // wait for the segment's bytes (bounded: a lost copy must not hang the GPU)
-    long long polls = 0;
-    bool ok = true;
-    while (!mbar_try_wait(&bars[st], (uint32_t)((it / NST) & 1))) {
-      if (++polls > WAIT_LIMIT) {
-        ok = false;
-        break;
-      }
-    }
-    if (__syncthreads_or(!ok)) {
-      if (tid == 0) {
-        atomicOr(sa.error, 1u);
-        // let the copies already issued land before the CTA leaves (bounded again)
-        for (int k = it; k < count && k < it + NST - 1; ++k) {
-          long long p2 = 0;
-          while (!mbar_try_wait(&bars[k % NST], (uint32_t)((k / NST) & 1)) && ++p2 < WAIT_LIMIT) {
-          }
-        }
-      }
-      break;
+    // After a wait gave up, the error is flagged and the remaining segments are
+    // passed through without waiting: every barrier is still met, nothing hangs.
+    if (!bad && !wait_phase(&full[st], (uint32_t)((it / NST) & 1))) {
+      atomicOr(sa.error, 1u);
+      bad = true;
     }
     const SegInfo g = info[st];
     const bool lid_row = sa.a.lateral == SIDE_LID && g.y == sa.a.ny - 1;
     float v[NSUM] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (tid < g.w) {
-      const uint32_t m = g.mslot >= 0 ? sa.masks[g.mslot + tid] : 0u;
-      stream_cell<S, COLL, REPORT, ODD>(sa.a, g, stage, tid, lid_row, m, v);
+      if (g.mslot < 0 && !lid_row) {
+        stream_cell<S, COLL, REPORT, ODD, true>(sa.a, g, stage, tid, false, 0u, v);
+      } else {
+        const uint32_t m = g.mslot >= 0 ? sa.masks[g.mslot + tid] : 0u;
+        stream_cell<S, COLL, REPORT, ODD, false>(sa.a, g, stage, tid, lid_row, m, v);
+      }
     }
     if (REPORT) {
 #pragma unroll
@@ -418,22 +447,17 @@ __global__ void __launch_bounds__(SW) stream_kernel(const __grid_constant__ Stre
         if (lane == 0) acc[k] = csum_add(acc[k], w);
       }
     }
-    fence_async_smem();  // this thread's shared-memory writes, before the bulk stores read them
-    __syncthreads();
-    if (warp == 0) {
-      issue_stores<S, ODD>(sa, tab, g, stage, lane);
-      const int nxt = it + NST - 1;
-      if (nxt < count)
-        issue_loads<S, ODD>(sa, tab, first + nxt * stride, stages + (nxt % NST) * L::STAGE, &bars[nxt % NST],
-                            &info[nxt % NST], lane);
+    if (ODD) {
+      consumer_sync();  // the edge elements were written by other threads
+      edge_stores<S, ODD>(sa, tab, g, stage, tid);
     }
-    edge_stores<S, ODD>(sa, tab, g, stage, tid);
+    fence_async_smem();  // this thread's shared-memory writes, before the bulk stores read them
+    mbar_arrive(&empty[st]);
   }
-  if (warp == 0) bulk_wait_all();
   if (REPORT) {
     if (lane == 0)
       for (int k = 0; k < NSUM; ++k) red[warp][k] = (double)acc[k].hi + (double)acc[k].lo;
-    __syncthreads();
+    consumer_sync();
     if (tid < NSUM) {
       double s = 0.0;
       for (int w = 0; w < SW / 32; ++w) s += red[w][tid];
