@@ -31,7 +31,6 @@
 namespace lbmk {
 
 constexpr int SW = 256;  // cells per segment = threads per CTA
-constexpr int NST = 3;   // pipeline stages
 constexpr uint32_t MASK_SOLID = 1u << 19;
 constexpr long long WAIT_LIMIT = 1ll << 20;  // mbarrier polls before a step gives up
 
@@ -66,7 +65,7 @@ __device__ __forceinline__ void bulk_store(void *dst, const void *src, uint32_t 
                : "memory");
 }
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_read_0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read_1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
@@ -193,6 +192,7 @@ struct Layout {
   static constexpr int H = 16 / (int)sizeof(S);        // halo: one 16-byte vector
   static constexpr int BUF = SW + 2 * H;               // elements per row-piece buffer
   static constexpr int STAGE = Q * BUF;                // elements per stage
+  static constexpr int NST = sizeof(S) == 8 ? 4 : 5;   // pipeline stages (two CTAs per SM fit below FP64)
   static constexpr size_t BYTES = (size_t)NST * STAGE * sizeof(S) + 2 * NST * sizeof(uint64_t);
 };
 
@@ -370,13 +370,14 @@ __device__ __forceinline__ void consumer_sync() {
 template <typename S, int COLL, bool REPORT, bool ODD>
 __global__ void __launch_bounds__(SW + 32) stream_kernel(const __grid_constant__ StreamArgs<S> sa) {
   using L = Layout<S>;
+  constexpr int NST = L::NST;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   S *stages = reinterpret_cast<S *>(smem_raw);
   uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + (size_t)NST * L::STAGE * sizeof(S));
   uint64_t *empty = full + NST;
   __shared__ double red[SW / 32][NSUM];
   __shared__ DirTab tab[Q];
-  __shared__ SegInfo info[NST];
+  __shared__ SegInfo info[L::NST];
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
   // this CTA's segments: blockIdx.x, blockIdx.x + gridDim.x, ...
@@ -394,8 +395,9 @@ __global__ void __launch_bounds__(SW + 32) stream_kernel(const __grid_constant__
   __syncthreads();
 
   if (warp == SW / 32) {
-    // producer warp
-    for (int k = 0; k < NST && k < count; ++k)
+    // producer warp: NST-1 segments ahead; a stage is refilled one iteration
+    // after its stores were issued, so they have drained by then
+    for (int k = 0; k < NST - 1 && k < count; ++k)
       issue_loads<S, ODD>(sa, tab, first + k * stride, stages + k * L::STAGE, &full[k], &info[k], lane);
     for (int it = 0; it < count; ++it) {
       const int st = it % NST;
@@ -404,11 +406,12 @@ __global__ void __launch_bounds__(SW + 32) stream_kernel(const __grid_constant__
         break;
       }
       issue_stores<S, ODD>(sa, tab, info[st], stages + st * L::STAGE, lane);
-      const int nxt = it + NST;
+      const int nxt = it + NST - 1;
       if (nxt < count) {
-        bulk_wait_read_0();  // this lane's stores out of the stage have read it
+        const int ns = nxt % NST;  // the stage of segment it-1 (or never used yet)
+        bulk_wait_read_1();        // this lane's stores of segment it-1 have read their buffer
         __syncwarp();
-        issue_loads<S, ODD>(sa, tab, first + nxt * stride, stages + st * L::STAGE, &full[st], &info[st], lane);
+        issue_loads<S, ODD>(sa, tab, first + nxt * stride, stages + ns * L::STAGE, &full[ns], &info[ns], lane);
       }
     }
     bulk_wait_all();
