@@ -366,7 +366,7 @@ __device__ __forceinline__ void consumer_sync() {
 
 // SW consumer threads (one cell each) plus one producer warp that owns the copies.
 // Stage s: `full` completes when the segment's bytes landed, `empty` when all
-// consumers are done with it (their updates fenced for the bulk stores).
+// consumer warps are done with it (their updates fenced for the bulk stores).
 template <typename S, int COLL, bool REPORT, bool ODD>
 __global__ void __launch_bounds__(SW + 32) stream_kernel(const __grid_constant__ StreamArgs<S> sa) {
   using L = Layout<S>;
@@ -387,7 +387,7 @@ __global__ void __launch_bounds__(SW + 32) stream_kernel(const __grid_constant__
   if (tid == 0) {
     for (int s = 0; s < NST; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], SW);
+      mbar_init(&empty[s], SW / 32);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     fence_async_smem();
@@ -455,7 +455,8 @@ __global__ void __launch_bounds__(SW + 32) stream_kernel(const __grid_constant__
       edge_stores<S, ODD>(sa, tab, g, stage, tid);
     }
     fence_async_smem();  // this thread's shared-memory writes, before the bulk stores read them
-    mbar_arrive(&empty[st]);
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[st]);  // one arrival per consumer warp
   }
   if (REPORT) {
     if (lane == 0)
