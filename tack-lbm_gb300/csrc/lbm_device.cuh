@@ -140,24 +140,30 @@ inline int cell_grid(long long n) {
 // ---------------------------------------------------------------------------
 // storage traits: load a deviation, store a deviation
 
-// load/store work on deviations d = f - w_q; load_value/store_value move the
-// population value f itself (host exchange), rounding once.
+// Population values in arithmetic: FP32 and FP64 storage keep f_q itself
+// (DEV = false); FP16/BF16 storage keeps the deviation f_q - w_q (DEV = true),
+// which is what the arithmetic then works on. load/store move values in that
+// representation; load_value/store_value move f_q itself (host exchange),
+// rounding once.
 template <> struct Store<float> {
   using T = float;
-  template <int q> __device__ static float load(const float *p) { return *p - wq(q); }
-  template <int q> __device__ static void store(float *p, float d) { *p = d + wq(q); }
+  static constexpr bool DEV = false;
+  template <int q> __device__ static float load(const float *p) { return *p; }
+  template <int q> __device__ static void store(float *p, float v) { *p = v; }
   template <int q> __device__ static double load_value(const float *p) { return (double)*p; }
   template <int q> __device__ static void store_value(float *p, double v) { *p = (float)v; }
 };
 template <> struct Store<double> {
   using T = double;
-  template <int q> __device__ static double load(const double *p) { return *p - (double)wq(q); }
-  template <int q> __device__ static void store(double *p, double d) { *p = d + (double)wq(q); }
+  static constexpr bool DEV = false;
+  template <int q> __device__ static double load(const double *p) { return *p; }
+  template <int q> __device__ static void store(double *p, double v) { *p = v; }
   template <int q> __device__ static double load_value(const double *p) { return *p; }
   template <int q> __device__ static void store_value(double *p, double v) { *p = v; }
 };
 template <> struct Store<__half> {
   using T = float;
+  static constexpr bool DEV = true;
   template <int q> __device__ static float load(const __half *p) { return __half2float(*p); }
   template <int q> __device__ static void store(__half *p, float d) { *p = __float2half_rn(d); }
   template <int q> __device__ static double load_value(const __half *p) {
@@ -169,6 +175,7 @@ template <> struct Store<__half> {
 };
 template <> struct Store<__nv_bfloat16> {
   using T = float;
+  static constexpr bool DEV = true;
   template <int q> __device__ static float load(const __nv_bfloat16 *p) { return __bfloat162float(*p); }
   template <int q> __device__ static void store(__nv_bfloat16 *p, float d) { *p = __float2bfloat16_rn(d); }
   template <int q> __device__ static double load_value(const __nv_bfloat16 *p) {
@@ -178,6 +185,12 @@ template <> struct Store<__nv_bfloat16> {
     *p = __double2bfloat16(v - (double)wq(q));
   }
 };
+
+// the value of population q at rest with rho = 1 in the representation DEV
+template <typename T, bool DEV>
+__host__ __device__ constexpr T rest_value(int q) {
+  return DEV ? T(0) : T(wq(q));
+}
 
 // ---------------------------------------------------------------------------
 // geometry: the reference's solid() tests evaluated in float32 with every
@@ -204,21 +217,69 @@ __device__ __forceinline__ bool solid(const Geo &g, int x, int y, int z) {
 }
 
 // ---------------------------------------------------------------------------
-// collision on deviations.
+// Moments, equilibrium, collisions and sponge on population values v_q
+// (v = f, or v = f - w with DEV).
 //
-// With delta_q = f_q - w_q, rho = 1 + drho, and X_q = 3 c.u + 4.5 (c.u)^2 - 1.5 u^2,
-// the equilibrium deviation is feq_q - w_q = w_q (drho + rho X_q) (lbm.py:52-55).
-// For a direction q and its opposite, with s = c_q.u:
-//   A = drho - 1.5 rho u^2 + 4.5 rho s^2,  B = 3 rho s,
-//   feq_q - w_q = w_q (A + B),  feq_opp - w_opp = w_q (A - B).
+// With rho = 1 + drho and s = c_q.u, the equilibrium of lbm.py:52-55 is
+//   feq_q = w_q (rho - 1.5 rho u^2 + 4.5 rho s^2 + 3 rho s);
+// in the value representation the constant rho becomes rv = DEV ? drho : rho.
+// The directions pair up as (q, opp q) = (2k+1, 2k+2), k = 0..8, with
+// feq = w (A + B) and w (A - B) for A = rv - 1.5 rho u^2 + 4.5 rho s^2,
+// B = 3 rho s. Sums P_k = v_q + v_opp and differences M_k = v_q - v_opp give
+// the density, momentum and second moments S_ab = sum c_a c_b v_q without
+// touching the 19 values again; for D3Q19 sum c_a c_b (feq - DEV w) =
+// rv/3 delta_ab + rho u_a u_b exactly, so the non-equilibrium stress of
+// lbm.py:81-91 is S_ab - rv/3 delta_ab - rho u_a u_b.
 
-// the 9 direction pairs (q, opp q) with q odd-numbered in the reference order
 __host__ __device__ constexpr int pq(int k) { return 2 * k + 1; }
 
 template <typename T>
 struct Moments {
   T drho, rho, ux, uy, uz;
 };
+
+// pairs k: q = 1 (1,0,0), 3 (0,1,0), 5 (0,0,1), 7 (1,1,0), 9 (1,-1,0),
+//          11 (1,0,1), 13 (1,0,-1), 15 (0,1,1), 17 (0,1,-1)
+template <typename T>
+struct Pairs {
+  T P[9], M[9];
+};
+
+template <typename T> __device__ __forceinline__ T rcp_fast(T v);
+template <> __device__ __forceinline__ float rcp_fast<float>(float v) { return __fdividef(1.0f, v); }
+template <> __device__ __forceinline__ double rcp_fast<double>(double v) { return 1.0 / v; }
+// square root of v >= 0 (0 maps to 0)
+template <typename T> __device__ __forceinline__ T sqrt_fast(T v);
+template <> __device__ __forceinline__ float sqrt_fast<float>(float v) { return v * rsqrtf(fmaxf(v, 1e-37f)); }
+template <> __device__ __forceinline__ double sqrt_fast<double>(double v) { return sqrt(v); }
+
+template <typename T, bool DEV>
+__device__ __forceinline__ Moments<T> moments(const T v[Q], bool fluid, Pairs<T> &pr) {
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    pr.P[k] = v[pq(k)] + v[pq(k) + 1];
+    pr.M[k] = v[pq(k)] - v[pq(k) + 1];
+  }
+  T sum = v[0];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) sum += pr.P[k];
+  Moments<T> m;
+  if (DEV) {
+    m.drho = sum + T(W_EXCESS);
+    m.rho = T(1) + m.drho;
+  } else {
+    m.rho = sum;
+    m.drho = sum - T(1);
+  }
+  const T jx = pr.M[0] + pr.M[3] + pr.M[4] + pr.M[5] + pr.M[6];
+  const T jy = pr.M[1] + pr.M[3] - pr.M[4] + pr.M[7] + pr.M[8];
+  const T jz = pr.M[2] + pr.M[5] - pr.M[6] + pr.M[7] - pr.M[8];
+  const T inv = fluid ? rcp_fast<T>(m.rho) : T(0);
+  m.ux = jx * inv;
+  m.uy = jy * inv;
+  m.uz = jz * inv;
+  return m;
+}
 
 template <typename T, int k>
 __device__ __forceinline__ T pair_dot(T ux, T uy, T uz) {
@@ -233,129 +294,109 @@ __device__ __forceinline__ T pair_dot(T ux, T uy, T uz) {
   return s;
 }
 
-// equilibrium deviations of all 19 directions
-template <typename T>
-__device__ __forceinline__ void feq_dev(T drho, T rho, T ux, T uy, T uz, T eq[Q]) {
-  const T base = drho - T(1.5) * rho * (ux * ux + uy * uy + uz * uz);
+// A and B of every pair (see above) and the rest population's equilibrium
+template <typename T, bool DEV>
+__device__ __forceinline__ void eq_pairs(T rv, T rho, T ux, T uy, T uz, T A[9], T B[9], T &eq0) {
+  const T base = rv - T(1.5) * rho * (ux * ux + uy * uy + uz * uz);
   const T r45 = T(4.5) * rho, r3 = T(3.0) * rho;
-  eq[0] = T(wq(0)) * base;
+  eq0 = T(wq(0)) * base;
+  static_for<9>([&](auto kc) {
+    constexpr int k = decltype(kc)::value;
+    const T sd = pair_dot<T, k>(ux, uy, uz);
+    A[k] = r45 * sd * sd + base;
+    B[k] = r3 * sd;
+  });
+}
+
+// equilibrium values of all 19 directions
+template <typename T, bool DEV>
+__device__ __forceinline__ void feq_val(T rv, T rho, T ux, T uy, T uz, T eq[Q]) {
+  T A[9], B[9];
+  eq_pairs<T, DEV>(rv, rho, ux, uy, uz, A, B, eq[0]);
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
-    const int q = pq(k);
-    T s;
-    switch (k) {
-      case 0: s = pair_dot<T, 0>(ux, uy, uz); break;
-      case 1: s = pair_dot<T, 1>(ux, uy, uz); break;
-      case 2: s = pair_dot<T, 2>(ux, uy, uz); break;
-      case 3: s = pair_dot<T, 3>(ux, uy, uz); break;
-      case 4: s = pair_dot<T, 4>(ux, uy, uz); break;
-      case 5: s = pair_dot<T, 5>(ux, uy, uz); break;
-      case 6: s = pair_dot<T, 6>(ux, uy, uz); break;
-      case 7: s = pair_dot<T, 7>(ux, uy, uz); break;
-      default: s = pair_dot<T, 8>(ux, uy, uz); break;
-    }
-    const T A = r45 * s * s + base;
-    const T B = r3 * s;
-    const T w = T(wq(q));
-    eq[q] = w * (A + B);
-    eq[q + 1] = w * (A - B);
+    const T w = T(wq(pq(k)));
+    eq[pq(k)] = w * (A[k] + B[k]);
+    eq[pq(k) + 1] = w * (A[k] - B[k]);
   }
 }
 
-template <typename T> __device__ __forceinline__ T fsqrt(T v);
-template <> __device__ __forceinline__ float fsqrt<float>(float v) { return __fsqrt_rn(v); }
-template <> __device__ __forceinline__ double fsqrt<double>(double v) { return sqrt(v); }
+template <typename T, bool DEV>
+__device__ __forceinline__ T rv_of(const Moments<T> &m) {
+  return DEV ? m.drho : m.rho;
+}
 
-// Relax the deviations d[] in place. Returns nothing; moments in m.
-// BGK (lbm.py:60-69), TRT + Smagorinsky (lbm.py:96-123), LES-BGK (lbm.py:126-139).
-template <typename T, int COLL>
-__device__ __forceinline__ void collide(T d[Q], const Moments<T> &m, T omega_bgk, T tau0,
+// Relax the values v[] in place: BGK (lbm.py:60-69), TRT + Smagorinsky
+// (lbm.py:96-123), LES-BGK (lbm.py:126-139).
+template <typename T, int COLL, bool DEV>
+__device__ __forceinline__ void collide(T v[Q], const Moments<T> &m, const Pairs<T> &pr, T omega_bgk, T tau0,
                                         T smag_c, T magic) {
-  T eq[Q];
-  feq_dev<T>(m.drho, m.rho, m.ux, m.uy, m.uz, eq);
+  T A[9], B[9], eq0;
+  eq_pairs<T, DEV>(rv_of<T, DEV>(m), m.rho, m.ux, m.uy, m.uz, A, B, eq0);
   if (COLL == COLL_BGK) {
+    v[0] += omega_bgk * (eq0 - v[0]);
 #pragma unroll
-    for (int q = 0; q < Q; ++q) d[q] = d[q] - omega_bgk * (d[q] - eq[q]);
+    for (int k = 0; k < 9; ++k) {
+      const int q = pq(k);
+      const T wA = T(wq(q)) * A[k], wB = T(wq(q)) * B[k];
+      v[q] += omega_bgk * ((wA + wB) - v[q]);
+      v[q + 1] += omega_bgk * ((wA - wB) - v[q + 1]);
+    }
     return;
   }
   // Smagorinsky relaxation time from the non-equilibrium stress (lbm.py:72-93)
-  T neq[Q];
-#pragma unroll
-  for (int q = 0; q < Q; ++q) neq[q] = d[q] - eq[q];
-  T pxx = T(0), pyy = T(0), pzz = T(0), pxy = T(0), pxz = T(0), pyz = T(0);
-#pragma unroll
-  for (int q = 1; q < Q; ++q) {
-    if (cx(q) != 0) pxx += neq[q];
-    if (cy(q) != 0) pyy += neq[q];
-    if (cz(q) != 0) pzz += neq[q];
-    if (cx(q) * cy(q) == 1) pxy += neq[q];
-    if (cx(q) * cy(q) == -1) pxy -= neq[q];
-    if (cx(q) * cz(q) == 1) pxz += neq[q];
-    if (cx(q) * cz(q) == -1) pxz -= neq[q];
-    if (cy(q) * cz(q) == 1) pyz += neq[q];
-    if (cy(q) * cz(q) == -1) pyz -= neq[q];
-  }
-  const T pi = fsqrt<T>(pxx * pxx + pyy * pyy + pzz * pzz + T(2) * (pxy * pxy + pxz * pxz + pyz * pyz));
-  const T tau = T(0.5) * (tau0 + fsqrt<T>(tau0 * tau0 + smag_c * pi / m.rho));
+  const T rv3 = rv_of<T, DEV>(m) * T(1.0 / 3.0);
+  const T rux = m.rho * m.ux, ruy = m.rho * m.uy;
+  const T pxx = (pr.P[0] + pr.P[3] + pr.P[4] + pr.P[5] + pr.P[6]) - rv3 - rux * m.ux;
+  const T pyy = (pr.P[1] + pr.P[3] + pr.P[4] + pr.P[7] + pr.P[8]) - rv3 - ruy * m.uy;
+  const T pzz = (pr.P[2] + pr.P[5] + pr.P[6] + pr.P[7] + pr.P[8]) - rv3 - m.rho * m.uz * m.uz;
+  const T pxy = (pr.P[3] - pr.P[4]) - rux * m.uy;
+  const T pxz = (pr.P[5] - pr.P[6]) - rux * m.uz;
+  const T pyz = (pr.P[7] - pr.P[8]) - ruy * m.uz;
+  const T pi = sqrt_fast<T>(pxx * pxx + pyy * pyy + pzz * pzz + T(2) * (pxy * pxy + pxz * pxz + pyz * pyz));
+  const T tau = T(0.5) * (tau0 + sqrt_fast<T>(tau0 * tau0 + smag_c * pi * rcp_fast<T>(m.rho)));
   if (COLL == COLL_LES) {
-    const T om = T(1) / tau;
+    const T om = rcp_fast<T>(tau);
+    v[0] += om * (eq0 - v[0]);
 #pragma unroll
-    for (int q = 0; q < Q; ++q) d[q] = d[q] - om * neq[q];
+    for (int k = 0; k < 9; ++k) {
+      const int q = pq(k);
+      const T wA = T(wq(q)) * A[k], wB = T(wq(q)) * B[k];
+      v[q] += om * ((wA + wB) - v[q]);
+      v[q + 1] += om * ((wA - wB) - v[q + 1]);
+    }
     return;
   }
   // TRT: even/odd parts relaxed at omega+ = 1/tau, omega- = 1/(magic/(tau-1/2)+1/2)
-  const T hp = T(0.5) / tau;
-  const T hm = T(0.5) / (magic / (tau - T(0.5)) + T(0.5));
-  d[0] = d[0] - T(2) * hp * neq[0];
+  const T hp = T(0.5) * rcp_fast<T>(tau);
+  const T hm = T(0.5) * rcp_fast<T>(magic * rcp_fast<T>(tau - T(0.5)) + T(0.5));
+  v[0] += T(2) * hp * (eq0 - v[0]);
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
     const int q = pq(k);
-    const T sym = hp * (neq[q] + neq[q + 1]);
-    const T anti = hm * (neq[q] - neq[q + 1]);
-    d[q] = d[q] - sym - anti;
-    d[q + 1] = d[q + 1] - sym + anti;
+    const T w2 = T(2) * T(wq(q));
+    const T sym = hp * (pr.P[k] - w2 * A[k]);
+    const T anti = hm * (pr.M[k] - w2 * B[k]);
+    v[q] = v[q] - sym - anti;
+    v[q + 1] = v[q + 1] - sym + anti;
   }
-}
-
-// moments of the deviations; fluid = 0 gives u = 0 (lbm.py:433-444)
-template <typename T>
-__device__ __forceinline__ Moments<T> moments(const T d[Q], bool fluid) {
-  T s = T(0), jx = T(0), jy = T(0), jz = T(0);
-#pragma unroll
-  for (int q = 0; q < Q; ++q) {
-    s += d[q];
-    if (cx(q) == 1) jx += d[q];
-    if (cx(q) == -1) jx -= d[q];
-    if (cy(q) == 1) jy += d[q];
-    if (cy(q) == -1) jy -= d[q];
-    if (cz(q) == 1) jz += d[q];
-    if (cz(q) == -1) jz -= d[q];
-  }
-  Moments<T> m;
-  m.drho = s + T(W_EXCESS);
-  m.rho = T(1) + m.drho;
-  const T inv = fluid ? T(1) / m.rho : T(0);
-  m.ux = jx * inv;
-  m.uy = jy * inv;
-  m.uz = jz * inv;
-  return m;
 }
 
 // Sponge blend toward (1, u0*fluid, 0, 0) (lbm.py:446-456):
-// out = feq(rho_s, u_s) + (1 - sigma)(post - feq(rho, u)), in deviations.
-template <typename T>
-__device__ __forceinline__ void sponge(T d[Q], const Moments<T> &m, T sigma, T u0fluid) {
+// out = feq(rho_s, u_s) + (1 - sigma)(post - feq(rho, u)), in values.
+template <typename T, bool DEV>
+__device__ __forceinline__ void sponge(T v[Q], const Moments<T> &m, T sigma, T u0fluid) {
   T e0[Q], e1[Q];
-  feq_dev<T>(m.drho, m.rho, m.ux, m.uy, m.uz, e0);
+  feq_val<T, DEV>(rv_of<T, DEV>(m), m.rho, m.ux, m.uy, m.uz, e0);
   const T drho_s = m.drho - sigma * m.drho;
   const T rho_s = T(1) + drho_s;
   const T ux_s = m.ux + sigma * (u0fluid - m.ux);
   const T uy_s = (T(1) - sigma) * m.uy;
   const T uz_s = (T(1) - sigma) * m.uz;
-  feq_dev<T>(drho_s, rho_s, ux_s, uy_s, uz_s, e1);
+  feq_val<T, DEV>(DEV ? drho_s : rho_s, rho_s, ux_s, uy_s, uz_s, e1);
   const T keep = T(1) - sigma;
 #pragma unroll
-  for (int q = 0; q < Q; ++q) d[q] = e1[q] + keep * (d[q] - e0[q]);
+  for (int q = 0; q < Q; ++q) v[q] = e1[q] + keep * (v[q] - e0[q]);
 }
 
 // ---------------------------------------------------------------------------
@@ -420,8 +461,13 @@ __device__ __forceinline__ int block_id() {
 // Every cell is fluid; x, y, z wrap periodically through per-lane / per-row
 // offsets. ODD selects the neighbour-reading half of the AA pair.
 
+// resident 128-thread blocks per SM the bulk kernel's register budget aims for
+#ifndef LBM_BULK_MIN_BLOCKS
+#define LBM_BULK_MIN_BLOCKS 1
+#endif
+
 template <typename S, int COLL, bool REPORT, bool ODD>
-__global__ void __launch_bounds__(BX * BY)
+__global__ void __launch_bounds__(BX * BY, LBM_BULK_MIN_BLOCKS)
 bulk_kernel(const __grid_constant__ StepArgs<S> a) {
   using T = typename Store<S>::T;
   const int bid = block_id();
@@ -454,11 +500,13 @@ bulk_kernel(const __grid_constant__ StepArgs<S> a) {
       if (ODD) d[q] = Store<S>::template load<q>(a.slot[opp(q)] + (idx + src_off(qc)));
       else d[q] = Store<S>::template load<q>(a.slot[q] + idx);
     });
-    const Moments<T> m = moments<T>(d, true);
-    collide<T, COLL>(d, m, a.omega_bgk, a.tau0, a.smag_c, a.magic);
+    constexpr bool DEV = Store<S>::DEV;
+    Pairs<T> pr;
+    const Moments<T> m = moments<T, DEV>(d, true, pr);
+    collide<T, COLL, DEV>(d, m, pr, a.omega_bgk, a.tau0, a.smag_c, a.magic);
     const T t = fmax(T(0), (T(x) - a.sponge_start) * a.inv_sponge_len);
     const T sigma = a.sponge_strength * t * t;
-    if (__any_sync(__activemask(), sigma != T(0))) sponge<T>(d, m, sigma, a.u0);
+    if (sigma != T(0)) sponge<T, DEV>(d, m, sigma, a.u0);
     static_for<Q>([&](auto pc) {
       constexpr int p = decltype(pc)::value;
       // population p moves to x + c_p, the source cell of direction opp(p) seen from x
@@ -560,8 +608,8 @@ generic_kernel(const __grid_constant__ StepArgs<S> a) {
       const T wall_term = T(6) * T(wq(q)) * k.cu;
       T val;
       if (here) {
-        // obstacle cell: streamed-in values, or its own w_q (deviation 0) on its bounce links
-        if (bb) val = wall_term;
+        // obstacle cell: streamed-in values, or its own w_q on its bounce links
+        if (bb) val = rest_value<T, Store<S>::DEV>(q) + wall_term;
         else val = ODD ? Store<S>::template load<q>(k.L) : Store<S>::template load<q>(a.slot[q] + idx);
       } else {
         S *src;
@@ -571,7 +619,7 @@ generic_kernel(const __grid_constant__ StepArgs<S> a) {
         val = bb ? got + wall_term : got;
         if (k.wall) {
           // momentum exchange (lbm.py:429-432); bounced = w_q + the deviation just read
-          const float hit = (float)(T(2) * (got + T(wq(q))) + wall_term);
+          const float hit = (float)(T(2) * (got + (Store<S>::DEV ? T(wq(q)) : T(0))) + wall_term);
           mx += hit * (float)(-cx(q));
           my += hit * (float)(-cy(q));
           mz += hit * (float)(-cz(q));
@@ -579,12 +627,14 @@ generic_kernel(const __grid_constant__ StepArgs<S> a) {
       }
       d[q] = val;
     });
-    const Moments<T> m = moments<T>(d, !here);
+    constexpr bool DEV = Store<S>::DEV;
+    Pairs<T> pr;
+    const Moments<T> m = moments<T, DEV>(d, !here, pr);
     if (!here) {
-      collide<T, COLL>(d, m, a.omega_bgk, a.tau0, a.smag_c, a.magic);
+      collide<T, COLL, DEV>(d, m, pr, a.omega_bgk, a.tau0, a.smag_c, a.magic);
       const T t = fmax(T(0), (T(x) - a.sponge_start) * a.inv_sponge_len);
       const T sigma = a.sponge_strength * t * t;
-      if (sigma != T(0)) sponge<T>(d, m, sigma, a.u0);
+      if (sigma != T(0)) sponge<T, DEV>(d, m, sigma, a.u0);
       static_for<Q>([&](auto pc) {
         constexpr int p = decltype(pc)::value;
         constexpr int o = opp(p);
@@ -661,7 +711,7 @@ __global__ void init_kernel(const __grid_constant__ StepArgs<S> a, float seed_am
     const float ang_z = 6.2831853f * (float)z / (float)a.nz;
     const T uy = T(seed_amp) * a.u0 * fluid * T(sinf(ang_x)) * T(cosf(ang_z));
     T eq[Q];
-    feq_dev<T>(T(0), T(1), ux, uy, T(0), eq);
+    feq_val<T, Store<S>::DEV>(Store<S>::DEV ? T(0) : T(1), T(1), ux, uy, T(0), eq);
     static_for<Q>([&](auto qc) {
       constexpr int q = decltype(qc)::value;
       Store<S>::template store<q>(a.slot[opp(q)] + idx, eq[q]);
@@ -700,7 +750,7 @@ __global__ void init_random_kernel(const __grid_constant__ StepArgs<S> a, float 
       uz = T(u_noise * (2.0f * uniform01(key, (uint64_t)idx, 4) - 1.0f));
     }
     T eq[Q];
-    feq_dev<T>(drho, T(1) + drho, ux, uy, uz, eq);
+    feq_val<T, Store<S>::DEV>(Store<S>::DEV ? drho : T(1) + drho, T(1) + drho, ux, uy, uz, eq);
     static_for<Q>([&](auto qc) {
       constexpr int q = decltype(qc)::value;
       Store<S>::template store<q>(a.slot[opp(q)] + idx, eq[q]);

@@ -318,12 +318,12 @@ __device__ __forceinline__ void stream_cell(const StepArgs<S> &a, const SegInfo 
       const Link<S> k = make_link<S, q>(a, x, g.y, g.z);
       const T wall_term = T(6) * T(wq(q)) * k.cu;
       if (here) {
-        val = wall_term;
+        val = rest_value<T, Store<S>::DEV>(q) + wall_term;
       } else {
         // parked on the previous step: own slot q (odd step) or the obstacle cell's slot (even)
         const T got = Store<S>::template load<q>(ODD ? a.slot[q] + idx : k.L);
         val = got + wall_term;
-        const float hit = (float)(T(2) * (got + T(wq(q))) + wall_term);
+        const float hit = (float)(T(2) * (got + (Store<S>::DEV ? T(wq(q)) : T(0))) + wall_term);
         mx += hit * (float)(-cx(q));
         my += hit * (float)(-cy(q));
         mz += hit * (float)(-cz(q));
@@ -332,16 +332,18 @@ __device__ __forceinline__ void stream_cell(const StepArgs<S> &a, const SegInfo 
     if (!PLAIN && cy(q) == -1 && lid_row) {
       // moving lid above the top row: the cell's own population comes back with the wall term
       const T lid_term = T(6) * T(wq(q)) * (T(cx(q)) * a.u_lid);
-      val = here ? lid_term : val + lid_term;
+      val = here ? rest_value<T, Store<S>::DEV>(q) + lid_term : val + lid_term;
     }
     d[q] = val;
   });
-  const Moments<T> mo = moments<T>(d, !here);
+  constexpr bool DEV = Store<S>::DEV;
+  Pairs<T> pr;
+  const Moments<T> mo = moments<T, DEV>(d, !here, pr);
   if (!here) {
-    collide<T, COLL>(d, mo, a.omega_bgk, a.tau0, a.smag_c, a.magic);
+    collide<T, COLL, DEV>(d, mo, pr, a.omega_bgk, a.tau0, a.smag_c, a.magic);
     const T t = fmax(T(0), (T(x) - a.sponge_start) * a.inv_sponge_len);
     const T sigma = a.sponge_strength * t * t;
-    if (sigma != T(0)) sponge<T>(d, mo, sigma, a.u0);
+    if (sigma != T(0)) sponge<T, DEV>(d, mo, sigma, a.u0);
     static_for<Q>([&](auto pc) {
       constexpr int p = decltype(pc)::value;
       // output p goes where input opp(p) came from
