@@ -225,13 +225,20 @@ __device__ __forceinline__ bool solid(const Geo &g, int x, int y, int z) {
 // in the value representation the constant rho becomes rv = DEV ? drho : rho.
 // The directions pair up as (q, opp q) = (2k+1, 2k+2), k = 0..8, with
 // feq = w (A + B) and w (A - B) for A = rv - 1.5 rho u^2 + 4.5 rho s^2,
-// B = 3 rho s. Sums P_k = v_q + v_opp and differences M_k = v_q - v_opp give
-// the density, momentum and second moments S_ab = sum c_a c_b v_q without
-// touching the 19 values again; for D3Q19 sum c_a c_b (feq - DEV w) =
-// rv/3 delta_ab + rho u_a u_b exactly, so the non-equilibrium stress of
-// lbm.py:81-91 is S_ab - rv/3 delta_ab - rho u_a u_b.
+// B = 3 rho s. The deviation pair sums D_k = f_q + f_opp - 2 w_q and the
+// differences M_k = f_q - f_opp give the density, the momentum and the
+// deviation second moments S_ab = sum c_a c_b (f_q - w_q) without cancellation.
+// The equilibrium's part of S_ab follows from the lattice moments of the
+// weights as uploaded (float32-rounded, lbm.py:48): with W2 = sum w c_x^2 and
+// W22 = sum w c_x^2 c_y^2,
+//   sum c_a c_a (feq - w) = W2 (drho - 1.5 rho u^2) + 4.5 rho (W2 u_a^2 + W22 (u^2 - u_a^2)),
+//   sum c_a c_b (feq - w) = 9 rho W22 u_a u_b (a != b),
+// which is drho/3 + rho u_a^2 and rho u_a u_b for exact weights; subtracting it
+// gives the non-equilibrium stress of lbm.py:81-91.
 
 __host__ __device__ constexpr int pq(int k) { return 2 * k + 1; }
+constexpr double W2 = 2.0 * (double)wq(1) + 8.0 * (double)wq(7);
+constexpr double W22 = 4.0 * (double)wq(7);
 
 template <typename T>
 struct Moments {
@@ -242,7 +249,7 @@ struct Moments {
 //          11 (1,0,1), 13 (1,0,-1), 15 (0,1,1), 17 (0,1,-1)
 template <typename T>
 struct Pairs {
-  T P[9], M[9];
+  T D[9], M[9];
 };
 
 template <typename T> __device__ __forceinline__ T rcp_fast(T v);
@@ -255,22 +262,19 @@ template <> __device__ __forceinline__ double sqrt_fast<double>(double v) { retu
 
 template <typename T, bool DEV>
 __device__ __forceinline__ Moments<T> moments(const T v[Q], bool fluid, Pairs<T> &pr) {
+  const T off0 = DEV ? T(0) : T(wq(0));
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
-    pr.P[k] = v[pq(k)] + v[pq(k) + 1];
+    const T offk = DEV ? T(0) : T(2) * T(wq(pq(k)));
+    pr.D[k] = (v[pq(k)] + v[pq(k) + 1]) - offk;
     pr.M[k] = v[pq(k)] - v[pq(k) + 1];
   }
-  T sum = v[0];
+  T sum = v[0] - off0;
 #pragma unroll
-  for (int k = 0; k < 9; ++k) sum += pr.P[k];
+  for (int k = 0; k < 9; ++k) sum += pr.D[k];
   Moments<T> m;
-  if (DEV) {
-    m.drho = sum + T(W_EXCESS);
-    m.rho = T(1) + m.drho;
-  } else {
-    m.rho = sum;
-    m.drho = sum - T(1);
-  }
+  m.drho = sum + T(W_EXCESS);
+  m.rho = T(1) + m.drho;
   const T jx = pr.M[0] + pr.M[3] + pr.M[4] + pr.M[5] + pr.M[6];
   const T jy = pr.M[1] + pr.M[3] - pr.M[4] + pr.M[7] + pr.M[8];
   const T jz = pr.M[2] + pr.M[5] - pr.M[6] + pr.M[7] - pr.M[8];
@@ -345,14 +349,17 @@ __device__ __forceinline__ void collide(T v[Q], const Moments<T> &m, const Pairs
     return;
   }
   // Smagorinsky relaxation time from the non-equilibrium stress (lbm.py:72-93)
-  const T rv3 = rv_of<T, DEV>(m) * T(1.0 / 3.0);
-  const T rux = m.rho * m.ux, ruy = m.rho * m.uy;
-  const T pxx = (pr.P[0] + pr.P[3] + pr.P[4] + pr.P[5] + pr.P[6]) - rv3 - rux * m.ux;
-  const T pyy = (pr.P[1] + pr.P[3] + pr.P[4] + pr.P[7] + pr.P[8]) - rv3 - ruy * m.uy;
-  const T pzz = (pr.P[2] + pr.P[5] + pr.P[6] + pr.P[7] + pr.P[8]) - rv3 - m.rho * m.uz * m.uz;
-  const T pxy = (pr.P[3] - pr.P[4]) - rux * m.uy;
-  const T pxz = (pr.P[5] - pr.P[6]) - rux * m.uz;
-  const T pyz = (pr.P[7] - pr.P[8]) - ruy * m.uz;
+  const T uxx = m.ux * m.ux, uyy = m.uy * m.uy, uzz = m.uz * m.uz, usq = uxx + uyy + uzz;
+  const T r45 = T(4.5) * m.rho;
+  const T iso = T(W2) * (m.drho - T(1.5) * m.rho * usq) + r45 * T(W22) * usq;
+  const T diag = r45 * T(W2 - W22);
+  const T offd = T(9) * m.rho * T(W22);
+  const T pxx = (pr.D[0] + pr.D[3] + pr.D[4] + pr.D[5] + pr.D[6]) - iso - diag * uxx;
+  const T pyy = (pr.D[1] + pr.D[3] + pr.D[4] + pr.D[7] + pr.D[8]) - iso - diag * uyy;
+  const T pzz = (pr.D[2] + pr.D[5] + pr.D[6] + pr.D[7] + pr.D[8]) - iso - diag * uzz;
+  const T pxy = (pr.D[3] - pr.D[4]) - offd * m.ux * m.uy;
+  const T pxz = (pr.D[5] - pr.D[6]) - offd * m.ux * m.uz;
+  const T pyz = (pr.D[7] - pr.D[8]) - offd * m.uy * m.uz;
   const T pi = sqrt_fast<T>(pxx * pxx + pyy * pyy + pzz * pzz + T(2) * (pxy * pxy + pxz * pxz + pyz * pyz));
   const T tau = T(0.5) * (tau0 + sqrt_fast<T>(tau0 * tau0 + smag_c * pi * rcp_fast<T>(m.rho)));
   if (COLL == COLL_LES) {
@@ -375,7 +382,8 @@ __device__ __forceinline__ void collide(T v[Q], const Moments<T> &m, const Pairs
   for (int k = 0; k < 9; ++k) {
     const int q = pq(k);
     const T w2 = T(2) * T(wq(q));
-    const T sym = hp * (pr.P[k] - w2 * A[k]);
+    // D_k - 2 w (A - rv + drho): the symmetric non-equilibrium part in deviations
+    const T sym = hp * (pr.D[k] - w2 * (A[k] - (DEV ? T(0) : T(1))));
     const T anti = hm * (pr.M[k] - w2 * B[k]);
     v[q] = v[q] - sym - anti;
     v[q + 1] = v[q + 1] - sym + anti;

@@ -212,11 +212,13 @@ def test_c1_one_step_and_200_steps(G, cs):
     f1 = O.step(cfg, f0).reshape(-1)
     assert O.weight_err(get(h, cfg.n), f1) <= TOL32
     if cs > 0:
-        # with the subgrid viscosity the flow is stable: 200 float32 steps against float64
+        # with the subgrid viscosity the flow is stable: 200 float32 steps against
+        # float64, allowed twice the drift of the reference's own arithmetic in float32
         h.call("lbm_run", 199, 0, None)
         f = O.run(cfg, f1, 199)
+        ref32 = O.weight_err(O.run(cfg, f1.astype(np.float32), 199, dtype=np.float32), f)
         err = O.weight_err(get(h, cfg.n), f)
-        assert err <= 2e-5, err
+        assert err <= max(2 * ref32, 1e-5), (err, ref32)
         return
     # plain TRT at Re 300 is unstable (lbm.py:99-101: beyond Re ~100): compare the
     # first 60 steps, then both runs must have blown up by step 200
