@@ -115,45 +115,16 @@ void obstacle_box(const lbm_config &g, Range r[3], bool &any) {
   }
 }
 
-lbm_status classify_blocks(lbm_solver *s) {
-  Ctx &c = s->c;
-  const lbm_config &g = c.cfg;
+// The obstacle's reach box, kept for the per-warp fast/general choice.
+void set_reach(Ctx &c) {
   Range box[3];
   bool any;
-  obstacle_box(g, box, any);
-  std::vector<uint8_t> flag((size_t)c.nblocks, 0);
-  std::vector<int> list;
-  const int last_by = (g.ny - 1) / lbmk::BY;
-  for (int z = 0; z < g.nz; ++z)
-    for (int by = 0; by < c.gy; ++by)
-      for (int bx = 0; bx < c.gx; ++bx) {
-        bool sp = false;
-        if (g.lateral != LBM_PERIODIC && (by == 0 || by == last_by)) sp = true;
-        if (g.vertical != LBM_PERIODIC && (z == 0 || z == g.nz - 1)) sp = true;
-        if (any) {
-          const int64_t x0 = (int64_t)bx * lbmk::BX, x1 = x0 + lbmk::BX - 1;
-          const int64_t y0 = (int64_t)by * lbmk::BY, y1 = y0 + lbmk::BY - 1;
-          if (x1 >= box[0].lo && x0 <= box[0].hi && y1 >= box[1].lo && y0 <= box[1].hi &&
-              z >= box[2].lo && z <= box[2].hi)
-            sp = true;
-        }
-        if (sp) {
-          const int bid = (z * c.gy + by) * c.gx + bx;
-          flag[(size_t)bid] = 1;
-          list.push_back(bid);
-        }
-      }
-  if (c.special) cudaFree(c.special);
-  if (c.special_list) cudaFree(c.special_list);
-  c.special = nullptr;
-  c.special_list = nullptr;
-  LBM_CUDA(cudaMalloc(&c.special, flag.size()));
-  LBM_CUDA(cudaMemcpy(c.special, flag.data(), flag.size(), cudaMemcpyHostToDevice));
-  c.nspecial = (int)list.size();
-  LBM_CUDA(cudaMalloc(&c.special_list, std::max<size_t>(1, list.size()) * sizeof(int)));
-  if (!list.empty())
-    LBM_CUDA(cudaMemcpy(c.special_list, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice));
-  return LBM_OK;
+  obstacle_box(c.cfg, box, any);
+  for (int k = 0; k < 3; ++k) {
+    c.reach_lo[k] = (int)std::max<int64_t>(box[k].lo, -1);
+    c.reach_hi[k] = (int)std::min<int64_t>(box[k].hi, 2147483646LL);
+  }
+  c.reach_any = any ? 1 : 0;
 }
 
 // Row segments of the bulk-copy kernel within reach of the obstacle get link masks.
@@ -274,8 +245,6 @@ void release(lbm_solver *s) {
   cudaFree(c.partials);
   cudaFree(c.stage);
   cudaFree(c.sums);
-  cudaFree(c.special);
-  cudaFree(c.special_list);
 }
 
 }  // namespace
@@ -427,12 +396,10 @@ lbm_status lbm_create(const lbm_config *cfg, lbm_solver **out) {
   if (e == cudaSuccess) e = cudaMemset(c.sums, 0, lbmk::NSUM * sizeof(double));
   if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("scratch: ") + cudaGetErrorString(e)));
   s->bytes += (c.partial_rows + lbmh::FINALIZE_BLOCKS + 1) * lbmk::NSUM * (int64_t)sizeof(double);
-  st = classify_blocks(s);
-  if (st != LBM_OK) return bail(st);
+  set_reach(c);
   st = classify_segments(s);
   if (st != LBM_OK) return bail(st);
   s->bytes += (int64_t)c.nseg * 4 + (int64_t)c.nmasked * (lbmk::SW + 1) * 4;
-  s->bytes += c.nblocks + (int64_t)c.nspecial * 4;
   release_output(c);
   e = cudaDeviceSynchronize();
   if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("create: ") + cudaGetErrorString(e)));
@@ -660,8 +627,8 @@ lbm_status lbm_set_obstacle(lbm_solver *s, int32_t kind, const double geo[7]) {
     return fail(LBM_ERR_CUDA, std::string("set_obstacle: ") + cudaGetErrorString(e));
   }
   s->c.cfg = g;
-  st = classify_blocks(s);
-  if (st == LBM_OK) st = classify_segments(s);
+  set_reach(s->c);
+  st = classify_segments(s);
   if (st == LBM_OK) {
     s->c.odd_next = 1;
     e = dispatch_import(s->c, tmp, dtype, 0);
@@ -775,20 +742,8 @@ lbm_status lbm_timing(lbm_solver *s, int32_t enable) {
   }
   c.ev_cap = cap;
   c.ev_used = 0;
-  // cells owned by each kernel
-  std::vector<int> list(c.nspecial);
-  if (c.nspecial)
-    LBM_CUDA(cudaMemcpy(list.data(), c.special_list, list.size() * sizeof(int), cudaMemcpyDeviceToHost));
-  int64_t gen = 0;
-  for (int packed : list) {
-    const int bx = packed % c.gx, by = (packed / c.gx) % c.gy;
-    const int64_t wx = std::min(lbmk::BX, c.cfg.nx - bx * lbmk::BX);
-    const int64_t wy = std::min(lbmk::BY, c.cfg.ny - by * lbmk::BY);
-    gen += wx * wy;
-  }
-  if (c.use_stream) gen = 0;
-  c.generic_cells = gen;
-  c.bulk_cells = c.n - gen;
+  c.generic_cells = 0;
+  c.bulk_cells = c.n;
   return LBM_OK;
 }
 
@@ -812,7 +767,7 @@ lbm_status lbm_timing_read(lbm_solver *s, double out[7]) {
   out[1] = c.ev_used;
   out[2] = (double)c.bulk_cells;
   out[3] = gen;
-  out[4] = (c.nspecial > 0 && !c.use_stream) ? c.ev_used : 0;
+  out[4] = 0;
   out[5] = (double)c.generic_cells;
   return LBM_OK;
 }

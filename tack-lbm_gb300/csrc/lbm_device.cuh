@@ -108,8 +108,8 @@ struct StepArgs {
   P omega_bgk, tau0, smag_c, magic;   // smag_c = 25.456 cs^2 (lbm.py:93)
   float *fld[13];
   double *partials;       // NSUM doubles per block (report steps)
-  const uint8_t *special; // 1 for blocks handled by the generic kernel
-  const int *special_list;
+  int reach_lo[3], reach_hi[3];  // cells that may be solid or next to solid lie in this box
+  int reach_any;                 // 0: no obstacle cell at all
   int gx, gy;             // grid dimensions in blocks (x, y)
 };
 
@@ -408,17 +408,40 @@ __device__ __forceinline__ void sponge(T v[Q], const Moments<T> &m, T sigma, T u
 }
 
 // ---------------------------------------------------------------------------
-// report-step reduction: 8 per-cell values summed in FP64 per block
+// Report-step sums. A float pair (Knuth's TwoSum) carries ~44 bits, so warp
+// sums of the float32 report fields lose nothing a float64 sum would keep; the
+// warps' pairs are then added in float64 (GB300's float64 pipe is narrow, so
+// float64 is kept to a handful of operations per block).
+
+struct CSum {
+  float hi, lo;
+};
+__device__ __forceinline__ CSum csum_add(CSum a, CSum b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bp = __fsub_rn(s, a.hi);
+  const float ap = __fsub_rn(s, bp);
+  const float e = __fadd_rn(__fsub_rn(a.hi, ap), __fsub_rn(b.hi, bp));
+  const float lo = __fadd_rn(__fadd_rn(a.lo, b.lo), e);
+  const float hi = __fadd_rn(s, lo);
+  return {hi, __fsub_rn(lo, __fsub_rn(hi, s))};
+}
+__device__ __forceinline__ CSum warp_csum(float v) {
+  CSum x{v, 0.f};
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    CSum y{__shfl_down_sync(0xffffffffu, x.hi, o), __shfl_down_sync(0xffffffffu, x.lo, o)};
+    x = csum_add(x, y);
+  }
+  return x;
+}
 
 __device__ __forceinline__ void block_sums(const float v[NSUM], double *partials, int bid) {
   __shared__ double red[BY][NSUM];
   const int lane = threadIdx.x, warp = threadIdx.y;
 #pragma unroll
   for (int k = 0; k < NSUM; ++k) {
-    double s = (double)v[k];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (lane == 0) red[warp][k] = s;
+    const CSum s = warp_csum(v[k]);
+    if (lane == 0) red[warp][k] = (double)s.hi + (double)s.lo;
   }
   __syncthreads();
   if (warp == 0 && lane < NSUM) {
@@ -460,74 +483,55 @@ __device__ __forceinline__ void diagnostics(float *const fld[13], int idx, const
   fld[12][idx] = mz;
 }
 
+
+// ---------------------------------------------------------------------------
+// Per-cell kernel bodies. ODD selects the neighbour-reading half of the AA pair.
+
 __device__ __forceinline__ int block_id() {
   return ((int)blockIdx.z * (int)gridDim.y + (int)blockIdx.y) * (int)gridDim.x + (int)blockIdx.x;
 }
 
-// ---------------------------------------------------------------------------
-// Bulk kernel: blocks with no obstacle cell within reach and no wall row.
-// Every cell is fluid; x, y, z wrap periodically through per-lane / per-row
-// offsets. ODD selects the neighbour-reading half of the AA pair.
-
-// resident 128-thread blocks per SM the bulk kernel's register budget aims for
-#ifndef LBM_BULK_MIN_BLOCKS
-#define LBM_BULK_MIN_BLOCKS 1
-#endif
-
+// Fast path: a fluid cell with no obstacle cell within reach, away from the
+// y/z walls. x, y, z wrap periodically through per-lane / per-row offsets.
 template <typename S, int COLL, bool REPORT, bool ODD>
-__global__ void __launch_bounds__(BX * BY, LBM_BULK_MIN_BLOCKS)
-bulk_kernel(const __grid_constant__ StepArgs<S> a) {
+__device__ __forceinline__ void fast_cell(const StepArgs<S> &a, int x, int y, int z, int idx, float v[NSUM]) {
   using T = typename Store<S>::T;
-  const int bid = block_id();
-  if (a.special[bid]) return;  // uniform per block
-  const int x = (int)blockIdx.x * BX + (int)threadIdx.x;
-  const int y = (int)blockIdx.y * BY + (int)threadIdx.y;
-  const int z = (int)blockIdx.z;
-  const bool active = x < a.nx && y < a.ny;
-  float v[NSUM] = {0, 0, 0, 0, 0, 0, 0, 0};
-  if (active) {
-    const int idx = (z * a.ny + y) * a.nx + x;
-    T d[Q];
-    int dxm = 0, dxp = 0, dym = 0, dyp = 0, dzm = 0, dzp = 0;
-    if (ODD) {
-      dxm = x == 0 ? a.nx - 1 : -1;
-      dxp = x == a.nx - 1 ? 1 - a.nx : 1;
-      dym = y == 0 ? (a.ny - 1) * a.nx : -a.nx;
-      dyp = y == a.ny - 1 ? -(a.ny - 1) * a.nx : a.nx;
-      dzm = z == 0 ? (a.nz - 1) * a.nxy : -a.nxy;
-      dzp = z == a.nz - 1 ? -(a.nz - 1) * a.nxy : a.nxy;
-    }
-    // offset of the cell x - c_q (the source of population q)
-    auto src_off = [&](auto qc) {
-      constexpr int q = decltype(qc)::value;
-      return (cx(q) == 1 ? dxm : cx(q) == -1 ? dxp : 0) + (cy(q) == 1 ? dym : cy(q) == -1 ? dyp : 0) +
-             (cz(q) == 1 ? dzm : cz(q) == -1 ? dzp : 0);
-    };
-    static_for<Q>([&](auto qc) {
-      constexpr int q = decltype(qc)::value;
-      if (ODD) d[q] = Store<S>::template load<q>(a.slot[opp(q)] + (idx + src_off(qc)));
-      else d[q] = Store<S>::template load<q>(a.slot[q] + idx);
-    });
-    constexpr bool DEV = Store<S>::DEV;
-    Pairs<T> pr;
-    const Moments<T> m = moments<T, DEV>(d, true, pr);
-    collide<T, COLL, DEV>(d, m, pr, a.omega_bgk, a.tau0, a.smag_c, a.magic);
-    const T t = fmax(T(0), (T(x) - a.sponge_start) * a.inv_sponge_len);
-    const T sigma = a.sponge_strength * t * t;
-    if (sigma != T(0)) sponge<T, DEV>(d, m, sigma, a.u0);
-    static_for<Q>([&](auto pc) {
-      constexpr int p = decltype(pc)::value;
-      // population p moves to x + c_p, the source cell of direction opp(p) seen from x
-      if (ODD) Store<S>::template store<p>(a.slot[p] + (idx + src_off(std::integral_constant<int, opp(p)>{})), d[p]);
-      else Store<S>::template store<p>(a.slot[opp(p)] + idx, d[p]);
-    });
-    if (REPORT) diagnostics<T>(a.fld, idx, m, 0.f, 0.f, 0.f, v);
+  constexpr bool DEV = Store<S>::DEV;
+  T d[Q];
+  int dxm = 0, dxp = 0, dym = 0, dyp = 0, dzm = 0, dzp = 0;
+  if (ODD) {
+    dxm = x == 0 ? a.nx - 1 : -1;
+    dxp = x == a.nx - 1 ? 1 - a.nx : 1;
+    dym = y == 0 ? (a.ny - 1) * a.nx : -a.nx;
+    dyp = y == a.ny - 1 ? -(a.ny - 1) * a.nx : a.nx;
+    dzm = z == 0 ? (a.nz - 1) * a.nxy : -a.nxy;
+    dzp = z == a.nz - 1 ? -(a.nz - 1) * a.nxy : a.nxy;
   }
-  if (REPORT) block_sums(v, a.partials, bid);
+  // offset of the cell x - c_q (the source of population q)
+  auto src_off = [&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    return (cx(q) == 1 ? dxm : cx(q) == -1 ? dxp : 0) + (cy(q) == 1 ? dym : cy(q) == -1 ? dyp : 0) +
+           (cz(q) == 1 ? dzm : cz(q) == -1 ? dzp : 0);
+  };
+  static_for<Q>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    if (ODD) d[q] = Store<S>::template load<q>(a.slot[opp(q)] + (idx + src_off(qc)));
+    else d[q] = Store<S>::template load<q>(a.slot[q] + idx);
+  });
+  Pairs<T> pr;
+  const Moments<T> m = moments<T, DEV>(d, true, pr);
+  collide<T, COLL, DEV>(d, m, pr, a.omega_bgk, a.tau0, a.smag_c, a.magic);
+  const T t = fmax(T(0), (T(x) - a.sponge_start) * a.inv_sponge_len);
+  const T sigma = a.sponge_strength * t * t;
+  if (sigma != T(0)) sponge<T, DEV>(d, m, sigma, a.u0);
+  static_for<Q>([&](auto pc) {
+    constexpr int p = decltype(pc)::value;
+    // population p moves to x + c_p, the source cell of direction opp(p) seen from x
+    if (ODD) Store<S>::template store<p>(a.slot[p] + (idx + src_off(std::integral_constant<int, opp(p)>{})), d[p]);
+    else Store<S>::template store<p>(a.slot[opp(p)] + idx, d[p]);
+  });
+  if (REPORT) diagnostics<T>(a.fld, idx, m, 0.f, 0.f, 0.f, v);
 }
-
-// ---------------------------------------------------------------------------
-// Generic kernel: the links of a cell evaluated one by one (lbm.py:410-432).
 
 template <typename S>
 struct Link {
@@ -537,8 +541,9 @@ struct Link {
   typename Store<S>::T cu;  // c_q . u_wall (bounce links only)
 };
 
+// geo = false skips the obstacle test (a cell with no obstacle cell within reach)
 template <typename S, int q>
-__device__ __forceinline__ Link<S> make_link(const StepArgs<S> &a, int x, int y, int z) {
+__device__ __forceinline__ Link<S> make_link(const StepArgs<S> &a, int x, int y, int z, bool geo = true) {
   using T = typename Store<S>::T;
   Link<S> k;
   int xs = x - cx(q);
@@ -563,7 +568,7 @@ __device__ __forceinline__ Link<S> make_link(const StepArgs<S> &a, int x, int y,
     rz = zs < 0 || zs >= a.nz;
     zs = rz ? z : zs;
   }
-  k.wall = !k.lid && solid(a.geo, xs, ys, zs);
+  k.wall = geo && !k.lid && solid(a.geo, xs, ys, zs);
   // the source population (cx, +-cy, +-cz) sits, in the even view, in the slot of its opposite
   constexpr int s00 = opp(q);
   constexpr int s01 = opp(dir(cx(q), cy(q), -cz(q)));
@@ -586,79 +591,92 @@ __device__ __forceinline__ Link<S> make_link(const StepArgs<S> &a, int x, int y,
   return k;
 }
 
-template <typename S>
-__device__ __forceinline__ void decode_special(const StepArgs<S> &a, int &bx, int &by, int &z) {
-  const int packed = a.special_list[blockIdx.x];
-  bx = packed % a.gx;
-  by = (packed / a.gx) % a.gy;
-  z = packed / (a.gx * a.gy);
+// General path: the links of a cell evaluated one by one (lbm.py:410-432):
+// walls, reflections, the lid, and - when geo - the obstacle.
+template <typename S, int COLL, bool REPORT, bool ODD>
+__device__ __forceinline__ void general_cell(const StepArgs<S> &a, int x, int y, int z, int idx, bool geo,
+                                             float v[NSUM]) {
+  using T = typename Store<S>::T;
+  constexpr bool DEV = Store<S>::DEV;
+  const bool here = geo && solid(a.geo, x, y, z);
+  if (here && !REPORT) return;
+  T d[Q];
+  float mx = 0.f, my = 0.f, mz = 0.f;
+  static_for<Q>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    const Link<S> k = make_link<S, q>(a, x, y, z, geo);
+    const bool bb = k.lid || k.wall;
+    const T wall_term = T(6) * T(wq(q)) * k.cu;
+    T val;
+    if (here) {
+      // obstacle cell: streamed-in values, or its own w_q on its bounce links
+      if (bb) val = rest_value<T, DEV>(q) + wall_term;
+      else val = ODD ? Store<S>::template load<q>(k.L) : Store<S>::template load<q>(a.slot[q] + idx);
+    } else {
+      S *src;
+      if (ODD) src = bb ? a.slot[q] + idx : k.L;
+      else src = k.wall ? k.L : a.slot[q] + idx;
+      const T got = Store<S>::template load<q>(src);
+      val = bb ? got + wall_term : got;
+      if (k.wall) {
+        // momentum exchange (lbm.py:429-432); bounced = the population just read
+        const float hit = (float)(T(2) * (got + (DEV ? T(wq(q)) : T(0))) + wall_term);
+        mx += hit * (float)(-cx(q));
+        my += hit * (float)(-cy(q));
+        mz += hit * (float)(-cz(q));
+      }
+    }
+    d[q] = val;
+  });
+  Pairs<T> pr;
+  const Moments<T> m = moments<T, DEV>(d, !here, pr);
+  if (!here) {
+    collide<T, COLL, DEV>(d, m, pr, a.omega_bgk, a.tau0, a.smag_c, a.magic);
+    const T t = fmax(T(0), (T(x) - a.sponge_start) * a.inv_sponge_len);
+    const T sigma = a.sponge_strength * t * t;
+    if (sigma != T(0)) sponge<T, DEV>(d, m, sigma, a.u0);
+    static_for<Q>([&](auto pc) {
+      constexpr int p = decltype(pc)::value;
+      constexpr int o = opp(p);
+      S *dst;
+      if (ODD) {
+        const Link<S> k = make_link<S, o>(a, x, y, z, geo);
+        dst = k.lid ? a.slot[o] + idx : k.L;
+      } else {
+        dst = a.slot[o] + idx;
+      }
+      Store<S>::template store<p>(dst, d[p]);
+    });
+  }
+  if (REPORT) diagnostics<T>(a.fld, idx, m, mx, my, mz, v);
 }
 
+// One step over the lattice: a warp is one row segment of 32 cells, so the
+// choice between the fast and the general path is uniform per warp.
+#ifndef LBM_STEP_MIN_BLOCKS
+#define LBM_STEP_MIN_BLOCKS 1
+#endif
+
 template <typename S, int COLL, bool REPORT, bool ODD>
-__global__ void __launch_bounds__(BX * BY)
-generic_kernel(const __grid_constant__ StepArgs<S> a) {
-  using T = typename Store<S>::T;
-  int bx, by, z;
-  decode_special(a, bx, by, z);
-  const int x = bx * BX + (int)threadIdx.x;
-  const int y = by * BY + (int)threadIdx.y;
-  const bool active = x < a.nx && y < a.ny;
+__global__ void __launch_bounds__(BX * BY, LBM_STEP_MIN_BLOCKS)
+step_kernel(const __grid_constant__ StepArgs<S> a) {
+  const int x0 = (int)blockIdx.x * BX;
+  const int x = x0 + (int)threadIdx.x;
+  const int y = (int)blockIdx.y * BY + (int)threadIdx.y;
+  const int z = (int)blockIdx.z;
   float v[NSUM] = {0, 0, 0, 0, 0, 0, 0, 0};
-  const bool here = active && solid(a.geo, x, y, z);
-  if (active && (REPORT || !here)) {
-    const int idx = (z * a.ny + y) * a.nx + x;
-    T d[Q];
-    float mx = 0.f, my = 0.f, mz = 0.f;
-    static_for<Q>([&](auto qc) {
-      constexpr int q = decltype(qc)::value;
-      const Link<S> k = make_link<S, q>(a, x, y, z);
-      const bool bb = k.lid || k.wall;
-      const T wall_term = T(6) * T(wq(q)) * k.cu;
-      T val;
-      if (here) {
-        // obstacle cell: streamed-in values, or its own w_q on its bounce links
-        if (bb) val = rest_value<T, Store<S>::DEV>(q) + wall_term;
-        else val = ODD ? Store<S>::template load<q>(k.L) : Store<S>::template load<q>(a.slot[q] + idx);
-      } else {
-        S *src;
-        if (ODD) src = bb ? a.slot[q] + idx : k.L;
-        else src = k.wall ? k.L : a.slot[q] + idx;
-        const T got = Store<S>::template load<q>(src);
-        val = bb ? got + wall_term : got;
-        if (k.wall) {
-          // momentum exchange (lbm.py:429-432); bounced = w_q + the deviation just read
-          const float hit = (float)(T(2) * (got + (Store<S>::DEV ? T(wq(q)) : T(0))) + wall_term);
-          mx += hit * (float)(-cx(q));
-          my += hit * (float)(-cy(q));
-          mz += hit * (float)(-cz(q));
-        }
-      }
-      d[q] = val;
-    });
-    constexpr bool DEV = Store<S>::DEV;
-    Pairs<T> pr;
-    const Moments<T> m = moments<T, DEV>(d, !here, pr);
-    if (!here) {
-      collide<T, COLL, DEV>(d, m, pr, a.omega_bgk, a.tau0, a.smag_c, a.magic);
-      const T t = fmax(T(0), (T(x) - a.sponge_start) * a.inv_sponge_len);
-      const T sigma = a.sponge_strength * t * t;
-      if (sigma != T(0)) sponge<T, DEV>(d, m, sigma, a.u0);
-      static_for<Q>([&](auto pc) {
-        constexpr int p = decltype(pc)::value;
-        constexpr int o = opp(p);
-        S *dst;
-        if (ODD) {
-          const Link<S> k = make_link<S, o>(a, x, y, z);
-          dst = k.lid ? a.slot[o] + idx : k.L;
-        } else {
-          dst = a.slot[o] + idx;
-        }
-        Store<S>::template store<p>(dst, d[p]);
-      });
+  if (y < a.ny) {
+    const bool wall_row = (a.lateral != SIDE_PERIODIC && (y == 0 || y == a.ny - 1)) ||
+                          (a.vertical != SIDE_PERIODIC && (z == 0 || z == a.nz - 1));
+    const bool near = a.reach_any && x0 + BX - 1 >= a.reach_lo[0] && x0 <= a.reach_hi[0] &&
+                      y >= a.reach_lo[1] && y <= a.reach_hi[1] && z >= a.reach_lo[2] && z <= a.reach_hi[2];
+    if (x < a.nx) {
+      const int idx = (z * a.ny + y) * a.nx + x;
+      if (!wall_row && !near) fast_cell<S, COLL, REPORT, ODD>(a, x, y, z, idx, v);
+      else general_cell<S, COLL, REPORT, ODD>(a, x, y, z, idx, near, v);
     }
-    if (REPORT) diagnostics<T>(a.fld, idx, m, mx, my, mz, v);
   }
-  if (REPORT) block_sums(v, a.partials, (z * a.gy + by) * a.gx + bx);
+  if (REPORT) block_sums(v, a.partials, block_id());
 }
 
 // ---------------------------------------------------------------------------

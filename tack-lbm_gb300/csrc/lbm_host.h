@@ -19,9 +19,7 @@ struct Ctx {
   double *partials;          // 8 doubles per block (report steps)
   double *stage;             // finalize stage: 8 doubles per finalize block
   double *sums;              // 8 doubles: the last report step's FP64 sums
-  uint8_t *special;          // per block: 1 when the generic kernel owns it
-  int *special_list;         // packed block ids ((z*gy + by)*gx + bx)
-  int nspecial;
+  int reach_lo[3], reach_hi[3], reach_any;  // cells that may be solid or next to solid
   int gx, gy;                // blocks along x and y (32 x 4 cells each)
   int64_t nblocks;           // gx*gy*nz
   int odd_next;              // 1: the next step reads neighbours (state in "even view")

@@ -38,8 +38,11 @@ StepArgs<S> make_args(const Ctx &c) {
   a.magic = (P)g.magic;
   for (int k = 0; k < LBM_NUM_FIELDS; ++k) a.fld[k] = c.fld[k];
   a.partials = c.partials;
-  a.special = c.special;
-  a.special_list = c.special_list;
+  for (int k = 0; k < 3; ++k) {
+    a.reach_lo[k] = c.reach_lo[k];
+    a.reach_hi[k] = c.reach_hi[k];
+  }
+  a.reach_any = c.reach_any;
   a.gx = c.gx;
   a.gy = c.gy;
   return a;
@@ -81,9 +84,8 @@ cudaError_t launch_variant(const Ctx &c, const StepArgs<S> &a, cudaStream_t st, 
   } else {
     const dim3 block(BX, BY);
     const dim3 grid(c.gx, c.gy, c.cfg.nz);
-    bulk_kernel<S, COLL, REPORT, ODD><<<grid, block, 0, st>>>(a);
+    step_kernel<S, COLL, REPORT, ODD><<<grid, block, 0, st>>>(a);
     if (ev) cudaEventRecord(ev[1], st);
-    if (c.nspecial > 0) generic_kernel<S, COLL, REPORT, ODD><<<c.nspecial, block, 0, st>>>(a);
     *rows = c.nblocks;
   }
   if (ev) cudaEventRecord(ev[2], st);

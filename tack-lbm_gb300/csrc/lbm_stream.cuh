@@ -69,33 +69,6 @@ __device__ __forceinline__ void bulk_wait_read_1() { asm volatile("cp.async.bulk
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-// ---------------------------------------------------------------------------
-// compensated float32 sums (Knuth's TwoSum): a float pair carries ~44 bits,
-// so the warp and segment sums of the report fields lose nothing a float64
-// sum would keep; float64 is used only across warps and CTAs.
-
-struct CSum {
-  float hi, lo;
-};
-__device__ __forceinline__ CSum csum_add(CSum a, CSum b) {
-  const float s = __fadd_rn(a.hi, b.hi);
-  const float bp = __fsub_rn(s, a.hi);
-  const float ap = __fsub_rn(s, bp);
-  const float e = __fadd_rn(__fsub_rn(a.hi, ap), __fsub_rn(b.hi, bp));
-  const float lo = __fadd_rn(__fadd_rn(a.lo, b.lo), e);
-  const float hi = __fadd_rn(s, lo);
-  return {hi, __fsub_rn(lo, __fsub_rn(hi, s))};
-}
-__device__ __forceinline__ CSum warp_csum(float v) {
-  CSum x{v, 0.f};
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    CSum y{__shfl_down_sync(0xffffffffu, x.hi, o), __shfl_down_sync(0xffffffffu, x.lo, o)};
-    x = csum_add(x, y);
-  }
-  return x;
-}
-
 template <typename S>
 struct StreamArgs {
   StepArgs<S> a;
