@@ -145,14 +145,15 @@ def max_over_ranks(value, dist, torch):
     return float(t.item())
 
 
-def make_solver(storage, device):
+def make_solver(storage, device, path):
     import lbm
     w = WORKLOAD
     return lbm.Solver(w["nx"], w["ny"], w["nz"], collision=w["collision"], obstacle=w["obstacle"],
                       reynolds=w["reynolds"], u0=w["u0"], diameter=w["diameter"],
                       device=f"cuda:{device}", lateral=w["lateral"], vertical=w["vertical"],
                       storage=storage, obstacle_center=w["center"], sponge_planes=w["sponge_planes"],
-                      init="random", seed=w["seed"], rho_sigma=w["rho_sigma"], u_noise=w["u_noise"])
+                      init="random", seed=w["seed"], rho_sigma=w["rho_sigma"], u_noise=w["u_noise"],
+                      kernel=path)
 
 
 def oracle_config():
@@ -260,6 +261,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16", "f64"])
+    ap.add_argument("--path", default="auto", choices=["auto", "simt", "bulkcopy"],
+                    help="step kernel: per-cell (simt), bulk-copy staged (bulkcopy), or the library's choice")
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -270,7 +273,7 @@ def main():
 
     world, rank, local, dist, torch = dist_setup(args.gpus)
     import lbm_native as N
-    s = make_solver(args.storage, local)
+    s = make_solver(args.storage, local, args.path)
     steps = min(args.steps, 4096)
     for _ in range(args.warmup):
         s.step()

@@ -20,6 +20,8 @@ Differences from the reference, all additive:
 * ``cs``, ``obstacle_center``, ``obstacle_size`` and ``sponge_start`` /
   ``sponge_planes`` / ``sponge_strength`` override the reference's fixed
   values (lbm.py:107, lbm.py:561, lbm.py:628-637), which stay the defaults;
+* ``kernel="simt"`` forces the per-cell step kernel instead of the
+  bulk-copy staged one;
 * populations are updated in place (AA pattern): ``f`` is a one-element list
   holding the current populations in the reference layout, read back from
   the GPU.
@@ -332,7 +334,7 @@ class Solver:
                  heat=False, prandtl=0.7, lateral="periodic", *, storage="f32",
                  vertical="periodic", cs=None, obstacle_center=None, obstacle_size=None,
                  sponge_start=None, sponge_planes=None, sponge_strength=1.0, u_lid=0.0,
-                 init="wave", seed=0, rho_sigma=1e-3, u_noise=0.01):
+                 init="wave", seed=0, rho_sigma=1e-3, u_noise=0.01, kernel="auto"):
         if heat:
             raise NotImplementedError("heat=True (the D3Q7 thermal block) is not part of this solver")
         self.device_index = 0 if device in ("cuda", None) else int(str(device).split(":")[-1])
@@ -358,6 +360,7 @@ class Solver:
         self.set_obstacle(obstacle, _apply=False)
         self.set_physics(collision, reynolds, _apply=False)
         cfg = _config(self.lat, self.phys, self.geo, self.flow, storage, self.device_index)
+        cfg.flags = {"auto": 0, "bulkcopy": 0, "simt": N.FLAG_SIMT}[kernel]
         self._h = N.Handle(cfg)
         n = self.lat.n
         self.fields = {}
