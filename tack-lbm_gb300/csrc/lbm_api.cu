@@ -115,8 +115,9 @@ void obstacle_box(const lbm_config &g, Range r[3], bool &any) {
   }
 }
 
-// The obstacle's reach box, kept for the per-warp fast/general choice.
-void set_reach(Ctx &c) {
+// The obstacle's reach box and the list of special warps (wall rows and the
+// reach box), which the general kernel updates beside the fast kernel.
+lbm_status set_reach(Ctx &c) {
   Range box[3];
   bool any;
   obstacle_box(c.cfg, box, any);
@@ -125,6 +126,30 @@ void set_reach(Ctx &c) {
     c.reach_hi[k] = (int)std::min<int64_t>(box[k].hi, 2147483646LL);
   }
   c.reach_any = any ? 1 : 0;
+  const lbm_config &g = c.cfg;
+  c.wx = (g.nx + lbmk::BX - 1) / lbmk::BX;
+  c.special_cells = 0;
+  std::vector<int> list;
+  for (int z = 0; z < g.nz; ++z)
+    for (int y = 0; y < g.ny; ++y)
+      for (int w = 0; w < c.wx; ++w) {
+        const int x0 = w * lbmk::BX;
+        const bool wall_row = (g.lateral != LBM_PERIODIC && (y == 0 || y == g.ny - 1)) ||
+                              (g.vertical != LBM_PERIODIC && (z == 0 || z == g.nz - 1));
+        const bool near = c.reach_any && x0 + lbmk::BX - 1 >= c.reach_lo[0] && x0 <= c.reach_hi[0] &&
+                          y >= c.reach_lo[1] && y <= c.reach_hi[1] && z >= c.reach_lo[2] && z <= c.reach_hi[2];
+        if (wall_row || near) {
+          list.push_back((z * g.ny + y) * c.wx + w);
+          c.special_cells += std::min(lbmk::BX, g.nx - x0);
+        }
+      }
+  cudaFree(c.special);
+  c.special = nullptr;
+  c.nspecial = (int)list.size();
+  LBM_CUDA(cudaMalloc(&c.special, std::max<size_t>(1, list.size()) * sizeof(int)));
+  if (!list.empty())
+    LBM_CUDA(cudaMemcpy(c.special, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice));
+  return LBM_OK;
 }
 
 // Row segments of the bulk-copy kernel within reach of the obstacle get link masks.
@@ -240,6 +265,10 @@ void release(lbm_solver *s) {
   cudaFree(c.seg_list);
   cudaFree(c.masks);
   cudaFree(c.error);
+  cudaFree(c.special);
+  if (c.side) cudaStreamDestroy(c.side);
+  if (c.fork) cudaEventDestroy(c.fork);
+  if (c.join) cudaEventDestroy(c.join);
   cudaFree(c.F);
   for (int k = 0; k < LBM_NUM_FIELDS; ++k) cudaFree(c.fld[k]);
   cudaFree(c.partials);
@@ -372,6 +401,17 @@ lbm_status lbm_create(const lbm_config *cfg, lbm_solver **out) {
       return fail(LBM_ERR_CUDA, std::string("cudaDeviceGetAttribute: ") + cudaGetErrorString(e0));
     }
   }
+  {
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    cudaError_t e0 = cudaStreamCreateWithPriority(&c.side, cudaStreamNonBlocking, hi);
+    if (e0 == cudaSuccess) e0 = cudaEventCreateWithFlags(&c.fork, cudaEventDisableTiming);
+    if (e0 == cudaSuccess) e0 = cudaEventCreateWithFlags(&c.join, cudaEventDisableTiming);
+    if (e0 != cudaSuccess) {
+      delete s;
+      return fail(LBM_ERR_CUDA, std::string("side stream: ") + cudaGetErrorString(e0));
+    }
+  }
   auto bail = [&](lbm_status e) {
     release(s);
     delete s;
@@ -387,7 +427,8 @@ lbm_status lbm_create(const lbm_config *cfg, lbm_solver **out) {
     if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("cudaMallocManaged: ") + cudaGetErrorString(e)));
     s->bytes += c.n * (int64_t)sizeof(float);
   }
-  c.partial_rows = std::max<int64_t>(c.nblocks, (int64_t)c.num_sms * 32);
+  // fast-kernel blocks plus at most one general block per four warps
+  c.partial_rows = std::max<int64_t>(2 * c.nblocks + 1, (int64_t)c.num_sms * 32);
   e = cudaMalloc(&c.partials, (size_t)c.partial_rows * lbmk::NSUM * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&c.error, sizeof(unsigned int));
   if (e == cudaSuccess) e = cudaMemset(c.error, 0, sizeof(unsigned int));
@@ -396,7 +437,8 @@ lbm_status lbm_create(const lbm_config *cfg, lbm_solver **out) {
   if (e == cudaSuccess) e = cudaMemset(c.sums, 0, lbmk::NSUM * sizeof(double));
   if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("scratch: ") + cudaGetErrorString(e)));
   s->bytes += (c.partial_rows + lbmh::FINALIZE_BLOCKS + 1) * lbmk::NSUM * (int64_t)sizeof(double);
-  set_reach(c);
+  st = set_reach(c);
+  if (st != LBM_OK) return bail(st);
   st = classify_segments(s);
   if (st != LBM_OK) return bail(st);
   s->bytes += (int64_t)c.nseg * 4 + (int64_t)c.nmasked * (lbmk::SW + 1) * 4;
@@ -627,8 +669,8 @@ lbm_status lbm_set_obstacle(lbm_solver *s, int32_t kind, const double geo[7]) {
     return fail(LBM_ERR_CUDA, std::string("set_obstacle: ") + cudaGetErrorString(e));
   }
   s->c.cfg = g;
-  set_reach(s->c);
-  st = classify_segments(s);
+  st = set_reach(s->c);
+  if (st == LBM_OK) st = classify_segments(s);
   if (st == LBM_OK) {
     s->c.odd_next = 1;
     e = dispatch_import(s->c, tmp, dtype, 0);
@@ -742,8 +784,8 @@ lbm_status lbm_timing(lbm_solver *s, int32_t enable) {
   }
   c.ev_cap = cap;
   c.ev_used = 0;
-  c.generic_cells = 0;
-  c.bulk_cells = c.n;
+  c.generic_cells = c.use_stream ? 0 : c.special_cells;
+  c.bulk_cells = c.n - c.generic_cells;
   return LBM_OK;
 }
 

@@ -491,6 +491,13 @@ __device__ __forceinline__ int block_id() {
   return ((int)blockIdx.z * (int)gridDim.y + (int)blockIdx.y) * (int)gridDim.x + (int)blockIdx.x;
 }
 
+// Is the warp [x0, x0+32) x {y} x {z} inside the obstacle's reach box?
+template <typename S>
+__device__ __forceinline__ bool near_obstacle(const StepArgs<S> &a, int x0, int y, int z) {
+  return a.reach_any && x0 + BX - 1 >= a.reach_lo[0] && x0 <= a.reach_hi[0] && y >= a.reach_lo[1] &&
+         y <= a.reach_hi[1] && z >= a.reach_lo[2] && z <= a.reach_hi[2];
+}
+
 // Fast path: a fluid cell with no obstacle cell within reach, away from the
 // y/z walls. x, y, z wrap periodically through per-lane / per-row offsets.
 template <typename S, int COLL, bool REPORT, bool ODD>
@@ -651,10 +658,19 @@ __device__ __forceinline__ void general_cell(const StepArgs<S> &a, int x, int y,
   if (REPORT) diagnostics<T>(a.fld, idx, m, mx, my, mz, v);
 }
 
-// One step over the lattice: a warp is one row segment of 32 cells, so the
-// choice between the fast and the general path is uniform per warp.
+// A warp is one row segment of 32 cells: the choice between the fast and the
+// general path is uniform per warp. "Special" warps (a y/z wall row, or the
+// obstacle's reach box) take the general path.
+template <typename S>
+__device__ __forceinline__ bool special_warp(const StepArgs<S> &a, int x0, int y, int z) {
+  const bool wall_row = (a.lateral != SIDE_PERIODIC && (y == 0 || y == a.ny - 1)) ||
+                        (a.vertical != SIDE_PERIODIC && (z == 0 || z == a.nz - 1));
+  return wall_row || near_obstacle(a, x0, y, z);
+}
+
+// Fast kernel: every warp that is not special (those are left to general_kernel).
 #ifndef LBM_STEP_MIN_BLOCKS
-#define LBM_STEP_MIN_BLOCKS 1
+#define LBM_STEP_MIN_BLOCKS 6
 #endif
 
 template <typename S, int COLL, bool REPORT, bool ODD>
@@ -665,18 +681,29 @@ step_kernel(const __grid_constant__ StepArgs<S> a) {
   const int y = (int)blockIdx.y * BY + (int)threadIdx.y;
   const int z = (int)blockIdx.z;
   float v[NSUM] = {0, 0, 0, 0, 0, 0, 0, 0};
-  if (y < a.ny) {
-    const bool wall_row = (a.lateral != SIDE_PERIODIC && (y == 0 || y == a.ny - 1)) ||
-                          (a.vertical != SIDE_PERIODIC && (z == 0 || z == a.nz - 1));
-    const bool near = a.reach_any && x0 + BX - 1 >= a.reach_lo[0] && x0 <= a.reach_hi[0] &&
-                      y >= a.reach_lo[1] && y <= a.reach_hi[1] && z >= a.reach_lo[2] && z <= a.reach_hi[2];
-    if (x < a.nx) {
-      const int idx = (z * a.ny + y) * a.nx + x;
-      if (!wall_row && !near) fast_cell<S, COLL, REPORT, ODD>(a, x, y, z, idx, v);
-      else general_cell<S, COLL, REPORT, ODD>(a, x, y, z, idx, near, v);
-    }
-  }
+  if (y < a.ny && x < a.nx && !special_warp(a, x0, y, z))
+    fast_cell<S, COLL, REPORT, ODD>(a, x, y, z, (z * a.ny + y) * a.nx + x, v);
   if (REPORT) block_sums(v, a.partials, block_id());
+}
+
+// General kernel: the special warps, four per block, from a list of
+// (z*ny + y)*wx + x0/32 row-segment ids. Report sums go to the partial rows
+// after the fast kernel's.
+template <typename S, int COLL, bool REPORT, bool ODD>
+__global__ void __launch_bounds__(BX * BY)
+general_kernel(const __grid_constant__ StepArgs<S> a, const int *list, int count, int wx, int row0) {
+  const int k = (int)blockIdx.x * BY + (int)threadIdx.y;
+  float v[NSUM] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (k < count) {
+    const int id = list[k];
+    const int x0 = (id % wx) * BX;
+    const int row = id / wx;
+    const int y = row % a.ny, z = row / a.ny;
+    const int x = x0 + (int)threadIdx.x;
+    if (x < a.nx)
+      general_cell<S, COLL, REPORT, ODD>(a, x, y, z, (z * a.ny + y) * a.nx + x, near_obstacle(a, x0, y, z), v);
+  }
+  if (REPORT) block_sums(v, a.partials, row0 + (int)blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------

@@ -20,6 +20,12 @@ struct Ctx {
   double *stage;             // finalize stage: 8 doubles per finalize block
   double *sums;              // 8 doubles: the last report step's FP64 sums
   int reach_lo[3], reach_hi[3], reach_any;  // cells that may be solid or next to solid
+  int *special;              // row-segment ids of the warps the general kernel updates
+  int nspecial;              // how many
+  int64_t special_cells;     // cells in them
+  int wx;                    // 32-cell row segments per row
+  cudaStream_t side;         // high-priority stream the general kernel overlaps on
+  cudaEvent_t fork, join;
   int gx, gy;                // blocks along x and y (32 x 4 cells each)
   int64_t nblocks;           // gx*gy*nz
   int odd_next;              // 1: the next step reads neighbours (state in "even view")
