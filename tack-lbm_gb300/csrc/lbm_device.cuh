@@ -452,7 +452,7 @@ __device__ __forceinline__ void block_sums(const float v[NSUM], double *partials
   }
 }
 
-// Diagnostics of one cell (lbm.py:493-513); v[] receives the values summed by monitors().
+// Diagnostics of one cell (lbm.py:493-513); the values monitors() sums are added to v[].
 template <typename T>
 __device__ __forceinline__ void diagnostics(float *const fld[13], int idx, const Moments<T> &m,
                                             float mx, float my, float mz, float v[NSUM]) {
@@ -463,21 +463,20 @@ __device__ __forceinline__ void diagnostics(float *const fld[13], int idx, const
   const float ox = fld[0][idx], oy = fld[1][idx], oz = fld[2][idx], op = fld[3][idx];
   const float ok = 0.5f * (ox * ox + oy * oy + oz * oz);
   const float dp = 3.0f * (p - op);
-  v[0] = dp * dp;
-  v[1] = (ux - ox) * (ux - ox);
-  v[2] = (uy - oy) * (uy - oy);
-  v[3] = (uz - oz) * (uz - oz);
-  v[4] = (ke - ok) * (ke - ok);
-  v[5] = mx;
-  v[6] = my;
-  v[7] = mz;
+  const float r[5] = {dp * dp, (ux - ox) * (ux - ox), (uy - oy) * (uy - oy), (uz - oz) * (uz - oz),
+                      (ke - ok) * (ke - ok)};
+#pragma unroll
+  for (int k = 0; k < 5; ++k) v[k] += r[k];
+  v[5] += mx;
+  v[6] += my;
+  v[7] += mz;
   fld[0][idx] = ux;
   fld[1][idx] = uy;
   fld[2][idx] = uz;
   fld[3][idx] = p;
   fld[4][idx] = sqrtf(ux * ux + uy * uy + uz * uz);
 #pragma unroll
-  for (int k = 0; k < 5; ++k) fld[5 + k][idx] = v[k];
+  for (int k = 0; k < 5; ++k) fld[5 + k][idx] = r[k];
   fld[10][idx] = mx;
   fld[11][idx] = my;
   fld[12][idx] = mz;
@@ -500,31 +499,49 @@ __device__ __forceinline__ bool near_obstacle(const StepArgs<S> &a, int x0, int 
 
 // Fast path: a fluid cell with no obstacle cell within reach, away from the
 // y/z walls. x, y, z wrap periodically through per-lane / per-row offsets.
-template <typename S, int COLL, bool REPORT, bool ODD>
-__device__ __forceinline__ void fast_cell(const StepArgs<S> &a, int x, int y, int z, int idx, float v[NSUM]) {
-  using T = typename Store<S>::T;
-  constexpr bool DEV = Store<S>::DEV;
-  T d[Q];
-  int dxm = 0, dxp = 0, dym = 0, dyp = 0, dzm = 0, dzp = 0;
+// fast_load issues the cell's 19 loads, fast_finish relaxes and stores it;
+// splitting them lets a thread keep the next cell's loads in flight.
+template <typename S>
+struct Offsets {
+  int dxm, dxp, dym, dyp, dzm, dzp;
+};
+
+template <typename S, bool ODD>
+__device__ __forceinline__ Offsets<S> fast_offsets(const StepArgs<S> &a, int x, int y, int z) {
+  Offsets<S> o{0, 0, 0, 0, 0, 0};
   if (ODD) {
-    dxm = x == 0 ? a.nx - 1 : -1;
-    dxp = x == a.nx - 1 ? 1 - a.nx : 1;
-    dym = y == 0 ? (a.ny - 1) * a.nx : -a.nx;
-    dyp = y == a.ny - 1 ? -(a.ny - 1) * a.nx : a.nx;
-    dzm = z == 0 ? (a.nz - 1) * a.nxy : -a.nxy;
-    dzp = z == a.nz - 1 ? -(a.nz - 1) * a.nxy : a.nxy;
+    o.dxm = x == 0 ? a.nx - 1 : -1;
+    o.dxp = x == a.nx - 1 ? 1 - a.nx : 1;
+    o.dym = y == 0 ? (a.ny - 1) * a.nx : -a.nx;
+    o.dyp = y == a.ny - 1 ? -(a.ny - 1) * a.nx : a.nx;
+    o.dzm = z == 0 ? (a.nz - 1) * a.nxy : -a.nxy;
+    o.dzp = z == a.nz - 1 ? -(a.nz - 1) * a.nxy : a.nxy;
   }
-  // offset of the cell x - c_q (the source of population q)
-  auto src_off = [&](auto qc) {
-    constexpr int q = decltype(qc)::value;
-    return (cx(q) == 1 ? dxm : cx(q) == -1 ? dxp : 0) + (cy(q) == 1 ? dym : cy(q) == -1 ? dyp : 0) +
-           (cz(q) == 1 ? dzm : cz(q) == -1 ? dzp : 0);
-  };
+  return o;
+}
+
+// offset of the cell x - c_q (the source of population q)
+template <int q, typename S>
+__device__ __forceinline__ int src_off(const Offsets<S> &o) {
+  return (cx(q) == 1 ? o.dxm : cx(q) == -1 ? o.dxp : 0) + (cy(q) == 1 ? o.dym : cy(q) == -1 ? o.dyp : 0) +
+         (cz(q) == 1 ? o.dzm : cz(q) == -1 ? o.dzp : 0);
+}
+
+template <typename S, bool ODD>
+__device__ __forceinline__ void fast_load(const StepArgs<S> &a, int idx, const Offsets<S> &o,
+                                          typename Store<S>::T d[Q]) {
   static_for<Q>([&](auto qc) {
     constexpr int q = decltype(qc)::value;
-    if (ODD) d[q] = Store<S>::template load<q>(a.slot[opp(q)] + (idx + src_off(qc)));
+    if (ODD) d[q] = Store<S>::template load<q>(a.slot[opp(q)] + (idx + src_off<q>(o)));
     else d[q] = Store<S>::template load<q>(a.slot[q] + idx);
   });
+}
+
+template <typename S, int COLL, bool REPORT, bool ODD>
+__device__ __forceinline__ void fast_finish(const StepArgs<S> &a, int x, int idx, const Offsets<S> &o,
+                                            typename Store<S>::T d[Q], float v[NSUM]) {
+  using T = typename Store<S>::T;
+  constexpr bool DEV = Store<S>::DEV;
   Pairs<T> pr;
   const Moments<T> m = moments<T, DEV>(d, true, pr);
   collide<T, COLL, DEV>(d, m, pr, a.omega_bgk, a.tau0, a.smag_c, a.magic);
@@ -534,7 +551,7 @@ __device__ __forceinline__ void fast_cell(const StepArgs<S> &a, int x, int y, in
   static_for<Q>([&](auto pc) {
     constexpr int p = decltype(pc)::value;
     // population p moves to x + c_p, the source cell of direction opp(p) seen from x
-    if (ODD) Store<S>::template store<p>(a.slot[p] + (idx + src_off(std::integral_constant<int, opp(p)>{})), d[p]);
+    if (ODD) Store<S>::template store<p>(a.slot[p] + (idx + src_off<opp(p)>(o)), d[p]);
     else Store<S>::template store<p>(a.slot[opp(p)] + idx, d[p]);
   });
   if (REPORT) diagnostics<T>(a.fld, idx, m, 0.f, 0.f, 0.f, v);
@@ -668,21 +685,53 @@ __device__ __forceinline__ bool special_warp(const StepArgs<S> &a, int x0, int y
   return wall_row || near_obstacle(a, x0, y, z);
 }
 
-// Fast kernel: every warp that is not special (those are left to general_kernel).
+// Fast kernel: every warp that is not special (those are left to
+// general_kernel). A thread updates ZCELLS cells, z = blockIdx.z + k*gridDim.z,
+// and issues the loads of the next one before relaxing the current one, so its
+// loads are in flight while it computes (two register buffers).
 #ifndef LBM_STEP_MIN_BLOCKS
-#define LBM_STEP_MIN_BLOCKS 6
+#define LBM_STEP_MIN_BLOCKS 4
 #endif
+constexpr int ZCELLS = 4;
 
 template <typename S, int COLL, bool REPORT, bool ODD>
 __global__ void __launch_bounds__(BX * BY, LBM_STEP_MIN_BLOCKS)
 step_kernel(const __grid_constant__ StepArgs<S> a) {
+  using T = typename Store<S>::T;
   const int x0 = (int)blockIdx.x * BX;
   const int x = x0 + (int)threadIdx.x;
   const int y = (int)blockIdx.y * BY + (int)threadIdx.y;
-  const int z = (int)blockIdx.z;
+  const int zs = (int)gridDim.z;
   float v[NSUM] = {0, 0, 0, 0, 0, 0, 0, 0};
-  if (y < a.ny && x < a.nx && !special_warp(a, x0, y, z))
-    fast_cell<S, COLL, REPORT, ODD>(a, x, y, z, (z * a.ny + y) * a.nx + x, v);
+  const bool live = y < a.ny && x < a.nx;
+  // cell k of this thread, if the fast kernel owns it
+  auto mine = [&](int k) {
+    const int z = (int)blockIdx.z + k * zs;
+    return live && z < a.nz && !special_warp(a, x0, y, z);
+  };
+  T A[Q], B[Q];
+  int zA = (int)blockIdx.z;
+  bool hasA = mine(0);
+  Offsets<S> oA = fast_offsets<S, ODD>(a, x, y, zA);
+  int iA = (zA * a.ny + y) * a.nx + x;
+  if (hasA) fast_load<S, ODD>(a, iA, oA, A);
+#pragma unroll
+  for (int k = 0; k < ZCELLS; k += 2) {
+    const int zB = zA + zs;
+    const bool hasB = k + 1 < ZCELLS && mine(k + 1);
+    const Offsets<S> oB = fast_offsets<S, ODD>(a, x, y, zB);
+    const int iB = (zB * a.ny + y) * a.nx + x;
+    if (hasB) fast_load<S, ODD>(a, iB, oB, B);
+    if (hasA) fast_finish<S, COLL, REPORT, ODD>(a, x, iA, oA, A, v);
+    if (k + 2 < ZCELLS) {
+      zA = zB + zs;
+      hasA = mine(k + 2);
+      oA = fast_offsets<S, ODD>(a, x, y, zA);
+      iA = (zA * a.ny + y) * a.nx + x;
+      if (hasA) fast_load<S, ODD>(a, iA, oA, A);
+    }
+    if (hasB) fast_finish<S, COLL, REPORT, ODD>(a, x, iB, oB, B, v);
+  }
   if (REPORT) block_sums(v, a.partials, block_id());
 }
 

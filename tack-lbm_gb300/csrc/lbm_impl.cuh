@@ -83,20 +83,21 @@ cudaError_t launch_variant(const Ctx &c, const StepArgs<S> &a, cudaStream_t st, 
     if (ev) cudaEventRecord(ev[1], st);
   } else {
     const dim3 block(BX, BY);
-    const dim3 grid(c.gx, c.gy, c.cfg.nz);
+    const dim3 grid(c.gx, c.gy, (c.cfg.nz + ZCELLS - 1) / ZCELLS);
+    const int64_t fblocks = (int64_t)grid.x * grid.y * grid.z;
     const int gblocks = (c.nspecial + BY - 1) / BY;
     if (gblocks > 0) {
       // the special warps run beside the fast kernel: their cells' memory is disjoint
       cudaEventRecord(c.fork, st);
       cudaStreamWaitEvent(c.side, c.fork, 0);
       general_kernel<S, COLL, REPORT, ODD><<<gblocks, block, 0, c.side>>>(a, c.special, c.nspecial, c.wx,
-                                                                         (int)c.nblocks);
+                                                                         (int)fblocks);
       cudaEventRecord(c.join, c.side);
     }
     step_kernel<S, COLL, REPORT, ODD><<<grid, block, 0, st>>>(a);
     if (ev) cudaEventRecord(ev[1], st);
     if (gblocks > 0) cudaStreamWaitEvent(st, c.join, 0);
-    *rows = c.nblocks + gblocks;
+    *rows = fblocks + gblocks;
   }
   if (ev) cudaEventRecord(ev[2], st);
   return cudaGetLastError();
