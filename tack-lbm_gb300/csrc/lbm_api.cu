@@ -115,33 +115,38 @@ void obstacle_box(const lbm_config &g, Range r[3], bool &any) {
   }
 }
 
-// The obstacle's reach box and the list of special warps (wall rows and the
-// reach box), which the general kernel updates beside the fast kernel.
+// The obstacle's reach box (clamped to the lattice), the link masks of the
+// 32-cell warps inside it, and the lid rows the general kernel updates.
 lbm_status set_reach(Ctx &c) {
   Range box[3];
   bool any;
   obstacle_box(c.cfg, box, any);
+  const lbm_config &g = c.cfg;
+  const int64_t dims[3] = {g.nx, g.ny, g.nz};
   for (int k = 0; k < 3; ++k) {
-    c.reach_lo[k] = (int)std::max<int64_t>(box[k].lo, -1);
-    c.reach_hi[k] = (int)std::min<int64_t>(box[k].hi, 2147483646LL);
+    c.reach_lo[k] = (int)std::max<int64_t>(box[k].lo, 0);
+    c.reach_hi[k] = (int)std::min<int64_t>(box[k].hi, dims[k] - 1);
+    if (c.reach_lo[k] > c.reach_hi[k]) any = false;
   }
   c.reach_any = any ? 1 : 0;
-  const lbm_config &g = c.cfg;
+  cudaFree(c.wmasks);
+  c.wmasks = nullptr;
+  if (c.reach_any) {
+    const int64_t nw = c.reach_hi[0] / lbmk::BX - c.reach_lo[0] / lbmk::BX + 1;
+    const int64_t words = nw * (c.reach_hi[1] - c.reach_lo[1] + 1) * (c.reach_hi[2] - c.reach_lo[2] + 1) *
+                          lbmk::BX;
+    LBM_CUDA(cudaMalloc(&c.wmasks, (size_t)words * sizeof(uint32_t)));
+    LBM_CUDA(lbmh::launch_warp_masks<float>(c, 0));
+    LBM_CUDA(cudaDeviceSynchronize());
+  }
   c.wx = (g.nx + lbmk::BX - 1) / lbmk::BX;
   c.special_cells = 0;
   std::vector<int> list;
-  for (int z = 0; z < g.nz; ++z)
-    for (int y = 0; y < g.ny; ++y)
+  if (g.lateral == LBM_LID)
+    for (int z = 0; z < g.nz; ++z)
       for (int w = 0; w < c.wx; ++w) {
-        const int x0 = w * lbmk::BX;
-        const bool wall_row = (g.lateral != LBM_PERIODIC && (y == 0 || y == g.ny - 1)) ||
-                              (g.vertical != LBM_PERIODIC && (z == 0 || z == g.nz - 1));
-        const bool near = c.reach_any && x0 + lbmk::BX - 1 >= c.reach_lo[0] && x0 <= c.reach_hi[0] &&
-                          y >= c.reach_lo[1] && y <= c.reach_hi[1] && z >= c.reach_lo[2] && z <= c.reach_hi[2];
-        if (wall_row || near) {
-          list.push_back((z * g.ny + y) * c.wx + w);
-          c.special_cells += std::min(lbmk::BX, g.nx - x0);
-        }
+        list.push_back((z * g.ny + (g.ny - 1)) * c.wx + w);
+        c.special_cells += std::min(lbmk::BX, g.nx - w * lbmk::BX);
       }
   cudaFree(c.special);
   c.special = nullptr;
@@ -266,6 +271,7 @@ void release(lbm_solver *s) {
   cudaFree(c.masks);
   cudaFree(c.error);
   cudaFree(c.special);
+  cudaFree(c.wmasks);
   if (c.side) cudaStreamDestroy(c.side);
   if (c.fork) cudaEventDestroy(c.fork);
   if (c.join) cudaEventDestroy(c.join);

@@ -110,6 +110,7 @@ struct StepArgs {
   double *partials;       // NSUM doubles per block (report steps)
   int reach_lo[3], reach_hi[3];  // cells that may be solid or next to solid lie in this box
   int reach_any;                 // 0: no obstacle cell at all
+  const uint32_t *masks;         // link masks of the warps in the reach box (32 words each)
   int gx, gy;             // grid dimensions in blocks (x, y)
 };
 
@@ -490,71 +491,137 @@ __device__ __forceinline__ int block_id() {
   return ((int)blockIdx.z * (int)gridDim.y + (int)blockIdx.y) * (int)gridDim.x + (int)blockIdx.x;
 }
 
-// Is the warp [x0, x0+32) x {y} x {z} inside the obstacle's reach box?
-template <typename S>
-__device__ __forceinline__ bool near_obstacle(const StepArgs<S> &a, int x0, int y, int z) {
-  return a.reach_any && x0 + BX - 1 >= a.reach_lo[0] && x0 <= a.reach_hi[0] && y >= a.reach_lo[1] &&
-         y <= a.reach_hi[1] && z >= a.reach_lo[2] && z <= a.reach_hi[2];
-}
 
-// Fast path: a fluid cell with no obstacle cell within reach, away from the
-// y/z walls. x, y, z wrap periodically through per-lane / per-row offsets.
-// fast_load issues the cell's 19 loads, fast_finish relaxes and stores it;
-// splitting them lets a thread keep the next cell's loads in flight.
+// Fast path. Offsets of the six neighbours with periodic wrap; on rows that
+// touch a free-slip wall (Row) a population that would come from beyond the
+// wall comes, reflected, from the row itself (lbm.py:355-369). Cells within
+// reach of the obstacle carry a link mask (bit q: population q bounces back,
+// MASK_SOLID: obstacle cell). A bounce-back input is read from where the cell
+// parked it on the previous step: its own slot q on an odd step, the odd-step
+// source location L(x, q) (inside the obstacle cell) on an even step.
 template <typename S>
 struct Offsets {
   int dxm, dxp, dym, dyp, dzm, dzp;
 };
 
-template <typename S, bool ODD>
-__device__ __forceinline__ Offsets<S> fast_offsets(const StepArgs<S> &a, int x, int y, int z) {
-  Offsets<S> o{0, 0, 0, 0, 0, 0};
-  if (ODD) {
-    o.dxm = x == 0 ? a.nx - 1 : -1;
-    o.dxp = x == a.nx - 1 ? 1 - a.nx : 1;
-    o.dym = y == 0 ? (a.ny - 1) * a.nx : -a.nx;
-    o.dyp = y == a.ny - 1 ? -(a.ny - 1) * a.nx : a.nx;
-    o.dzm = z == 0 ? (a.nz - 1) * a.nxy : -a.nxy;
-    o.dzp = z == a.nz - 1 ? -(a.nz - 1) * a.nxy : a.nxy;
-  }
+struct Row {
+  bool ylo, yhi, zlo, zhi;  // reflections at free-slip walls below y = 0 / above y = ny-1 / z
+};
+
+constexpr uint32_t MASK_SOLID = 1u << 19;
+constexpr uint32_t MASK_LINKS = MASK_SOLID - 1;
+
+template <typename S>
+__device__ __forceinline__ Offsets<S> cell_offsets(const StepArgs<S> &a, int x, int y, int z) {
+  Offsets<S> o;
+  o.dxm = x == 0 ? a.nx - 1 : -1;
+  o.dxp = x == a.nx - 1 ? 1 - a.nx : 1;
+  o.dym = y == 0 ? (a.ny - 1) * a.nx : -a.nx;
+  o.dyp = y == a.ny - 1 ? -(a.ny - 1) * a.nx : a.nx;
+  o.dzm = z == 0 ? (a.nz - 1) * a.nxy : -a.nxy;
+  o.dzp = z == a.nz - 1 ? -(a.nz - 1) * a.nxy : a.nxy;
   return o;
 }
 
-// offset of the cell x - c_q (the source of population q)
-template <int q, typename S>
-__device__ __forceinline__ int src_off(const Offsets<S> &o) {
-  return (cx(q) == 1 ? o.dxm : cx(q) == -1 ? o.dxp : 0) + (cy(q) == 1 ? o.dym : cy(q) == -1 ? o.dyp : 0) +
-         (cz(q) == 1 ? o.dzm : cz(q) == -1 ? o.dzp : 0);
+template <typename S>
+__device__ __forceinline__ Row row_of(const StepArgs<S> &a, int y, int z) {
+  Row r;
+  r.ylo = a.lateral != SIDE_PERIODIC && y == 0;
+  r.yhi = a.lateral == SIDE_SLIP && y == a.ny - 1;
+  r.zlo = a.vertical != SIDE_PERIODIC && z == 0;
+  r.zhi = a.vertical != SIDE_PERIODIC && z == a.nz - 1;
+  return r;
 }
 
-template <typename S, bool ODD>
-__device__ __forceinline__ void fast_load(const StepArgs<S> &a, int idx, const Offsets<S> &o,
-                                          typename Store<S>::T d[Q]) {
+// L(x, q): where population q of the cell streams from (odd steps read it there)
+template <int q, bool SPECIAL, typename S>
+__device__ __forceinline__ S *src_loc(const StepArgs<S> &a, int idx, const Offsets<S> &o, const Row &r) {
+  const int xp = cx(q) == 1 ? o.dxm : cx(q) == -1 ? o.dxp : 0;
+  const int yp = cy(q) == 1 ? o.dym : cy(q) == -1 ? o.dyp : 0;
+  const int zp = cz(q) == 1 ? o.dzm : cz(q) == -1 ? o.dzp : 0;
+  if (!SPECIAL) return a.slot[opp(q)] + (idx + xp + yp + zp);
+  const bool ry = (cy(q) == 1 && r.ylo) || (cy(q) == -1 && r.yhi);
+  const bool rz = (cz(q) == 1 && r.zlo) || (cz(q) == -1 && r.zhi);
+  constexpr int s00 = opp(q);
+  constexpr int s01 = opp(dir(cx(q), cy(q), -cz(q)));
+  constexpr int s10 = opp(dir(cx(q), -cy(q), cz(q)));
+  constexpr int s11 = opp(dir(cx(q), -cy(q), -cz(q)));
+  S *base = ry ? (rz ? a.slot[s11] : a.slot[s10]) : (rz ? a.slot[s01] : a.slot[s00]);
+  return base + (idx + xp + (ry ? 0 : yp) + (rz ? 0 : zp));
+}
+
+// moving-wall term 6 w_q c_q.u_w of a bounce link at its midpoint (lbm.py:417-428)
+template <int q, typename S>
+__device__ __forceinline__ typename Store<S>::T wall_term(const StepArgs<S> &a, int x, int y) {
+  using T = typename Store<S>::T;
+  if (a.geo.kind != OBS_CYL) return T(0);
+  const T xm = T(x) - T(0.5) * T(cx(q));
+  const T ym = T(y) - T(0.5) * T(cy(q));
+  const T vx = a.omega_rot * (-(ym - a.wall_oy) * a.wall_inv_r);
+  const T vy = a.omega_rot * ((xm - a.wall_ox) * a.wall_inv_r);
+  return T(6) * T(wq(q)) * (T(cx(q)) * vx + T(cy(q)) * vy);
+}
+
+template <typename S, bool ODD, bool SPECIAL>
+__device__ __forceinline__ void fast_load(const StepArgs<S> &a, int idx, const Offsets<S> &o, const Row &r,
+                                          uint32_t m, typename Store<S>::T d[Q]) {
   static_for<Q>([&](auto qc) {
     constexpr int q = decltype(qc)::value;
-    if (ODD) d[q] = Store<S>::template load<q>(a.slot[opp(q)] + (idx + src_off<q>(o)));
-    else d[q] = Store<S>::template load<q>(a.slot[q] + idx);
+    S *own = a.slot[q] + idx;
+    const S *addr;
+    if (!SPECIAL) {
+      addr = ODD ? src_loc<q, false>(a, idx, o, r) : own;
+    } else {
+      const bool b = (m >> q) & 1u;
+      S *src = src_loc<q, true>(a, idx, o, r);
+      addr = ODD ? (b ? own : src) : (b ? src : own);
+    }
+    d[q] = Store<S>::template load<q>(addr);
   });
 }
 
-template <typename S, int COLL, bool REPORT, bool ODD>
-__device__ __forceinline__ void fast_finish(const StepArgs<S> &a, int x, int idx, const Offsets<S> &o,
-                                            typename Store<S>::T d[Q], float v[NSUM]) {
+template <typename S, int COLL, bool REPORT, bool ODD, bool SPECIAL>
+__device__ __forceinline__ void fast_finish(const StepArgs<S> &a, int x, int y, int idx, const Offsets<S> &o,
+                                            const Row &r, uint32_t m, typename Store<S>::T d[Q], float v[NSUM]) {
   using T = typename Store<S>::T;
   constexpr bool DEV = Store<S>::DEV;
+  const bool here = SPECIAL && (m & MASK_SOLID);
+  float mx = 0.f, my = 0.f, mz = 0.f;
+  if (SPECIAL && (m & MASK_LINKS)) {
+    // bounce-back links (lbm.py:426-432): the value read is the cell's own
+    // population coming back, plus the moving-wall term
+    static_for<Q>([&](auto qc) {
+      constexpr int q = decltype(qc)::value;
+      if ((m >> q) & 1u) {
+        const T wt = wall_term<q>(a, x, y);
+        if (here) {
+          d[q] = rest_value<T, DEV>(q) + wt;
+        } else {
+          const T got = d[q];
+          d[q] = got + wt;
+          const float hit = (float)(T(2) * (got + (DEV ? T(wq(q)) : T(0))) + wt);
+          mx += hit * (float)(-cx(q));
+          my += hit * (float)(-cy(q));
+          mz += hit * (float)(-cz(q));
+        }
+      }
+    });
+  }
   Pairs<T> pr;
-  const Moments<T> m = moments<T, DEV>(d, true, pr);
-  collide<T, COLL, DEV>(d, m, pr, a.omega_bgk, a.tau0, a.smag_c, a.magic);
-  const T t = fmax(T(0), (T(x) - a.sponge_start) * a.inv_sponge_len);
-  const T sigma = a.sponge_strength * t * t;
-  if (sigma != T(0)) sponge<T, DEV>(d, m, sigma, a.u0);
-  static_for<Q>([&](auto pc) {
-    constexpr int p = decltype(pc)::value;
-    // population p moves to x + c_p, the source cell of direction opp(p) seen from x
-    if (ODD) Store<S>::template store<p>(a.slot[p] + (idx + src_off<opp(p)>(o)), d[p]);
-    else Store<S>::template store<p>(a.slot[opp(p)] + idx, d[p]);
-  });
-  if (REPORT) diagnostics<T>(a.fld, idx, m, 0.f, 0.f, 0.f, v);
+  const Moments<T> mo = moments<T, DEV>(d, !here, pr);
+  if (!here) {
+    collide<T, COLL, DEV>(d, mo, pr, a.omega_bgk, a.tau0, a.smag_c, a.magic);
+    const T t = fmax(T(0), (T(x) - a.sponge_start) * a.inv_sponge_len);
+    const T sigma = a.sponge_strength * t * t;
+    if (sigma != T(0)) sponge<T, DEV>(d, mo, sigma, a.u0);
+    static_for<Q>([&](auto pc) {
+      constexpr int p = decltype(pc)::value;
+      // population p moves to x + c_p: the odd-step source location of direction opp(p)
+      if (ODD) Store<S>::template store<p>(src_loc<opp(p), SPECIAL>(a, idx, o, r), d[p]);
+      else Store<S>::template store<p>(a.slot[opp(p)] + idx, d[p]);
+    });
+  }
+  if (REPORT) diagnostics<T>(a.fld, idx, mo, mx, my, mz, v);
 }
 
 template <typename S>
@@ -675,24 +742,29 @@ __device__ __forceinline__ void general_cell(const StepArgs<S> &a, int x, int y,
   if (REPORT) diagnostics<T>(a.fld, idx, m, mx, my, mz, v);
 }
 
-// A warp is one row segment of 32 cells: the choice between the fast and the
-// general path is uniform per warp. "Special" warps (a y/z wall row, or the
-// obstacle's reach box) take the general path.
+// A warp is one row segment of 32 cells, so every choice below is uniform per warp.
+
+// Is the warp [x0, x0+32) x {y} x {z} inside the obstacle's reach box?
+// Returns its first link-mask word, or -1.
 template <typename S>
-__device__ __forceinline__ bool special_warp(const StepArgs<S> &a, int x0, int y, int z) {
-  const bool wall_row = (a.lateral != SIDE_PERIODIC && (y == 0 || y == a.ny - 1)) ||
-                        (a.vertical != SIDE_PERIODIC && (z == 0 || z == a.nz - 1));
-  return wall_row || near_obstacle(a, x0, y, z);
+__device__ __forceinline__ int mask_slot(const StepArgs<S> &a, int x0, int y, int z) {
+  if (!a.reach_any || x0 + BX - 1 < a.reach_lo[0] || x0 > a.reach_hi[0] || y < a.reach_lo[1] ||
+      y > a.reach_hi[1] || z < a.reach_lo[2] || z > a.reach_hi[2])
+    return -1;
+  const int w0 = a.reach_lo[0] / BX, nw = a.reach_hi[0] / BX - w0 + 1;
+  const int nyr = a.reach_hi[1] - a.reach_lo[1] + 1;
+  return (((z - a.reach_lo[2]) * nyr + (y - a.reach_lo[1])) * nw + (x0 / BX - w0)) * BX;
 }
 
-// Fast kernel: every warp that is not special (those are left to
-// general_kernel). A thread updates ZCELLS cells, z = blockIdx.z + k*gridDim.z,
-// and issues the loads of the next one before relaxing the current one, so its
-// loads are in flight while it computes (two register buffers).
+// The lid row (the top row under LBM_LID) is left to general_kernel.
+template <typename S>
+__device__ __forceinline__ bool lid_row(const StepArgs<S> &a, int y) {
+  return a.lateral == SIDE_LID && y == a.ny - 1;
+}
+
 #ifndef LBM_STEP_MIN_BLOCKS
-#define LBM_STEP_MIN_BLOCKS 4
+#define LBM_STEP_MIN_BLOCKS 5
 #endif
-constexpr int ZCELLS = 4;
 
 template <typename S, int COLL, bool REPORT, bool ODD>
 __global__ void __launch_bounds__(BX * BY, LBM_STEP_MIN_BLOCKS)
@@ -701,38 +773,45 @@ step_kernel(const __grid_constant__ StepArgs<S> a) {
   const int x0 = (int)blockIdx.x * BX;
   const int x = x0 + (int)threadIdx.x;
   const int y = (int)blockIdx.y * BY + (int)threadIdx.y;
-  const int zs = (int)gridDim.z;
+  const int z = (int)blockIdx.z;
   float v[NSUM] = {0, 0, 0, 0, 0, 0, 0, 0};
-  const bool live = y < a.ny && x < a.nx;
-  // cell k of this thread, if the fast kernel owns it
-  auto mine = [&](int k) {
-    const int z = (int)blockIdx.z + k * zs;
-    return live && z < a.nz && !special_warp(a, x0, y, z);
-  };
-  T A[Q], B[Q];
-  int zA = (int)blockIdx.z;
-  bool hasA = mine(0);
-  Offsets<S> oA = fast_offsets<S, ODD>(a, x, y, zA);
-  int iA = (zA * a.ny + y) * a.nx + x;
-  if (hasA) fast_load<S, ODD>(a, iA, oA, A);
-#pragma unroll
-  for (int k = 0; k < ZCELLS; k += 2) {
-    const int zB = zA + zs;
-    const bool hasB = k + 1 < ZCELLS && mine(k + 1);
-    const Offsets<S> oB = fast_offsets<S, ODD>(a, x, y, zB);
-    const int iB = (zB * a.ny + y) * a.nx + x;
-    if (hasB) fast_load<S, ODD>(a, iB, oB, B);
-    if (hasA) fast_finish<S, COLL, REPORT, ODD>(a, x, iA, oA, A, v);
-    if (k + 2 < ZCELLS) {
-      zA = zB + zs;
-      hasA = mine(k + 2);
-      oA = fast_offsets<S, ODD>(a, x, y, zA);
-      iA = (zA * a.ny + y) * a.nx + x;
-      if (hasA) fast_load<S, ODD>(a, iA, oA, A);
+  if (y < a.ny && !lid_row(a, y) && x < a.nx) {
+    const int idx = (z * a.ny + y) * a.nx + x;
+    const Row r = row_of(a, y, z);
+    const int ms = mask_slot(a, x0, y, z);
+    const Offsets<S> o = cell_offsets(a, x, y, z);
+    T d[Q];
+    if (!(r.ylo || r.yhi || r.zlo || r.zhi) && ms < 0) {
+      fast_load<S, ODD, false>(a, idx, o, r, 0u, d);
+      fast_finish<S, COLL, REPORT, ODD, false>(a, x, y, idx, o, r, 0u, d, v);
+    } else {
+      const uint32_t m = ms >= 0 ? a.masks[ms + (int)threadIdx.x] : 0u;
+      if (REPORT || !(m & MASK_SOLID)) {
+        fast_load<S, ODD, true>(a, idx, o, r, m, d);
+        fast_finish<S, COLL, REPORT, ODD, true>(a, x, y, idx, o, r, m, d, v);
+      }
     }
-    if (hasB) fast_finish<S, COLL, REPORT, ODD>(a, x, iB, oB, B, v);
   }
   if (REPORT) block_sums(v, a.partials, block_id());
+}
+
+// Link masks of the warps within the obstacle's reach, one warp per 32 cells.
+template <typename S>
+__global__ void warp_mask_kernel(const __grid_constant__ StepArgs<S> a, uint32_t *masks) {
+  const int x0 = (int)blockIdx.x * BX;
+  const int y = (int)blockIdx.y, z = (int)blockIdx.z;
+  const int ms = mask_slot(a, x0, y, z);
+  if (ms < 0) return;
+  const int x = x0 + (int)threadIdx.x;
+  uint32_t m = 0;
+  if (x < a.nx) {
+    if (solid(a.geo, x, y, z)) m |= MASK_SOLID;
+    static_for<Q>([&](auto qc) {
+      constexpr int q = decltype(qc)::value;
+      if (make_link<S, q>(a, x, y, z).wall) m |= 1u << q;
+    });
+  }
+  masks[ms + (int)threadIdx.x] = m;
 }
 
 // General kernel: the special warps, four per block, from a list of
@@ -750,7 +829,7 @@ general_kernel(const __grid_constant__ StepArgs<S> a, const int *list, int count
     const int y = row % a.ny, z = row / a.ny;
     const int x = x0 + (int)threadIdx.x;
     if (x < a.nx)
-      general_cell<S, COLL, REPORT, ODD>(a, x, y, z, (z * a.ny + y) * a.nx + x, near_obstacle(a, x0, y, z), v);
+      general_cell<S, COLL, REPORT, ODD>(a, x, y, z, (z * a.ny + y) * a.nx + x, mask_slot(a, x0, y, z) >= 0, v);
   }
   if (REPORT) block_sums(v, a.partials, row0 + (int)blockIdx.x);
 }

@@ -20,7 +20,8 @@ struct Ctx {
   double *stage;             // finalize stage: 8 doubles per finalize block
   double *sums;              // 8 doubles: the last report step's FP64 sums
   int reach_lo[3], reach_hi[3], reach_any;  // cells that may be solid or next to solid
-  int *special;              // row-segment ids of the warps the general kernel updates
+  uint32_t *wmasks;          // link masks of the 32-cell warps within the obstacle's reach
+  int *special;              // row-segment ids of the warps the general kernel updates (lid rows)
   int nspecial;              // how many
   int64_t special_cells;     // cells in them
   int wx;                    // 32-cell row segments per row
@@ -60,6 +61,7 @@ template <typename S> cudaError_t launch_init_random(const Ctx &c, double rho_si
 template <typename S> cudaError_t launch_import(const Ctx &c, const void *src, int dtype, cudaStream_t st);
 template <typename S> cudaError_t launch_export(const Ctx &c, void *dst, int dtype, cudaStream_t st);
 template <typename S> cudaError_t launch_link_masks(const Ctx &c, cudaStream_t st);
+template <typename S> cudaError_t launch_warp_masks(const Ctx &c, cudaStream_t st);
 
 cudaError_t launch_finalize(const Ctx &c, int64_t rows, cudaStream_t st);
 cudaError_t launch_mask(const Ctx &c, uint8_t *dst_dev, cudaStream_t st);

@@ -43,6 +43,7 @@ StepArgs<S> make_args(const Ctx &c) {
     a.reach_hi[k] = c.reach_hi[k];
   }
   a.reach_any = c.reach_any;
+  a.masks = c.wmasks;
   a.gx = c.gx;
   a.gy = c.gy;
   return a;
@@ -83,7 +84,7 @@ cudaError_t launch_variant(const Ctx &c, const StepArgs<S> &a, cudaStream_t st, 
     if (ev) cudaEventRecord(ev[1], st);
   } else {
     const dim3 block(BX, BY);
-    const dim3 grid(c.gx, c.gy, (c.cfg.nz + ZCELLS - 1) / ZCELLS);
+    const dim3 grid(c.gx, c.gy, c.cfg.nz);
     const int64_t fblocks = (int64_t)grid.x * grid.y * grid.z;
     const int gblocks = (c.nspecial + BY - 1) / BY;
     if (gblocks > 0) {
@@ -123,6 +124,13 @@ cudaError_t launch_step(const Ctx &c, bool report, cudaStream_t st) {
   }
   if (e != cudaSuccess) return e;
   return report ? launch_finalize(c, rows, st) : cudaSuccess;
+}
+
+template <typename S>
+cudaError_t launch_warp_masks(const Ctx &c, cudaStream_t st) {
+  if (!c.reach_any) return cudaSuccess;
+  warp_mask_kernel<S><<<dim3(c.gx, c.cfg.ny, c.cfg.nz), BX, 0, st>>>(make_args<S>(c), c.wmasks);
+  return cudaGetLastError();
 }
 
 template <typename S>
@@ -172,6 +180,7 @@ cudaError_t launch_export(const Ctx &c, void *dst, int dtype, cudaStream_t st) {
   template cudaError_t launch_init_random<S>(const Ctx &, double, double, uint64_t, cudaStream_t); \
   template cudaError_t launch_import<S>(const Ctx &, const void *, int, cudaStream_t);        \
   template cudaError_t launch_export<S>(const Ctx &, void *, int, cudaStream_t);                \
-  template cudaError_t launch_link_masks<S>(const Ctx &, cudaStream_t);
+  template cudaError_t launch_link_masks<S>(const Ctx &, cudaStream_t);                       \
+  template cudaError_t launch_warp_masks<S>(const Ctx &, cudaStream_t);
 
 }  // namespace lbmh

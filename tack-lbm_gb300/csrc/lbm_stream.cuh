@@ -31,7 +31,6 @@
 namespace lbmk {
 
 constexpr int SW = 256;  // cells per segment = threads per CTA
-constexpr uint32_t MASK_SOLID = 1u << 19;
 constexpr long long WAIT_LIMIT = 1ll << 20;  // mbarrier polls before a step gives up
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
