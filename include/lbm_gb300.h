@@ -83,10 +83,12 @@ typedef struct lbm_config {
     int32_t flags;               /* LBM_FLAG_* */
 } lbm_config;
 
-/* lbm_config.flags: use the per-cell kernels instead of the bulk-copy kernel
- * (which needs nx*sizeof(storage) in 16-byte pieces; without them the per-cell
- * kernels are used anyway). */
+/* lbm_config.flags: LBM_FLAG_BULKCOPY selects the bulk-copy (TMA) staged step
+ * kernel instead of the default per-cell kernel; it needs rows that split into
+ * 16-byte pieces (nx*sizeof(storage) % 16 == 0), otherwise the per-cell kernel
+ * runs. LBM_FLAG_SIMT asks for the per-cell kernel explicitly. */
 #define LBM_FLAG_SIMT 1
+#define LBM_FLAG_BULKCOPY 2
 
 typedef struct lbm_solver lbm_solver;
 

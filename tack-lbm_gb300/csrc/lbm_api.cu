@@ -395,8 +395,8 @@ lbm_status lbm_create(const lbm_config *cfg, lbm_solver **out) {
     // the bulk-copy kernel moves 16-byte pieces: rows must split into them
     const int h = 16 / (int)storage_bytes(cfg->storage);
     const int tail = cfg->nx % lbmk::SW;
-    c.use_stream = !(cfg->flags & LBM_FLAG_SIMT) && cfg->nx % h == 0 && cfg->nx >= 2 * h &&
-                   (tail == 0 || tail >= 2 * h);
+    c.use_stream = (cfg->flags & LBM_FLAG_BULKCOPY) && !(cfg->flags & LBM_FLAG_SIMT) && cfg->nx % h == 0 &&
+                   cfg->nx >= 2 * h && (tail == 0 || tail >= 2 * h);
     c.nseg_x = (cfg->nx + lbmk::SW - 1) / lbmk::SW;
     c.nseg = c.nseg_x * cfg->ny * cfg->nz;
   }
@@ -791,7 +791,7 @@ lbm_status lbm_timing(lbm_solver *s, int32_t enable) {
   c.ev_cap = cap;
   c.ev_used = 0;
   c.generic_cells = c.use_stream ? 0 : c.special_cells;
-  c.bulk_cells = c.n - c.generic_cells;
+  c.bulk_cells = c.n - c.generic_cells;  // the dominant kernel's cells
   return LBM_OK;
 }
 
@@ -816,6 +816,7 @@ lbm_status lbm_timing_read(lbm_solver *s, double out[7]) {
   out[2] = (double)c.bulk_cells;
   out[3] = gen;
   out[4] = 0;
+  out[5] = (double)c.generic_cells;
   out[5] = (double)c.generic_cells;
   return LBM_OK;
 }

@@ -20,8 +20,8 @@ Differences from the reference, all additive:
 * ``cs``, ``obstacle_center``, ``obstacle_size`` and ``sponge_start`` /
   ``sponge_planes`` / ``sponge_strength`` override the reference's fixed
   values (lbm.py:107, lbm.py:561, lbm.py:628-637), which stay the defaults;
-* ``kernel="simt"`` forces the per-cell step kernel instead of the
-  bulk-copy staged one;
+* ``kernel="bulkcopy"`` selects the bulk-copy (TMA) staged step kernel
+  instead of the default per-cell one;
 * populations are updated in place (AA pattern): ``f`` is a one-element list
   holding the current populations in the reference layout, read back from
   the GPU.
@@ -360,7 +360,7 @@ class Solver:
         self.set_obstacle(obstacle, _apply=False)
         self.set_physics(collision, reynolds, _apply=False)
         cfg = _config(self.lat, self.phys, self.geo, self.flow, storage, self.device_index)
-        cfg.flags = {"auto": 0, "bulkcopy": 0, "simt": N.FLAG_SIMT}[kernel]
+        cfg.flags = {"auto": 0, "bulkcopy": N.FLAG_BULKCOPY, "simt": N.FLAG_SIMT}[kernel]
         self._h = N.Handle(cfg)
         n = self.lat.n
         self.fields = {}

@@ -31,11 +31,11 @@ def G():
     return G
 
 
-def native_handle(cfg, storage="f32", simt=False):
-    """A solver for cfg; simt=True forces the per-cell kernels instead of the bulk-copy kernel."""
+def native_handle(cfg, storage="f32", bulkcopy=False):
+    """A solver for cfg; bulkcopy=True selects the bulk-copy (TMA) staged step kernel."""
     import lbm_native as N
     c = N.Config()
-    c.flags = N.FLAG_SIMT if simt else 0
+    c.flags = N.FLAG_BULKCOPY if bulkcopy else 0
     c.nx, c.ny, c.nz = cfg.nx, cfg.ny, cfg.nz
     c.collision = N.COLLISION[cfg.collision]
     c.obstacle = N.OBSTACLE[cfg.obstacle]
@@ -126,14 +126,14 @@ def test_trt_ref_through_kernel_entry(G):
 
 
 PATHS = [False, True]
-PATH_IDS = ["bulkcopy", "simt"]
+PATH_IDS = ["percell", "bulkcopy"]
 
 
-@pytest.mark.parametrize("simt", PATHS, ids=PATH_IDS)
+@pytest.mark.parametrize("bulkcopy", PATHS, ids=PATH_IDS)
 @pytest.mark.parametrize("case", list(goldens.step_cases()), ids=lambda c: c["name"])
-def test_golden_step(G, case, simt):
+def test_golden_step(G, case, bulkcopy):
     cfg = case["cfg"]
-    h = native_handle(cfg, simt=simt)
+    h = native_handle(cfg, bulkcopy=bulkcopy)
     assert np.array_equal(gpu_mask(h, cfg.n), case["solid"])
     put(h, case["f_in"])
     set_fields(h, case["prev"])
@@ -144,12 +144,12 @@ def test_golden_step(G, case, simt):
         check_fields(get_fields(h, cfg.n), case["fields"], case["name"])
 
 
-@pytest.mark.parametrize("simt", PATHS, ids=PATH_IDS)
+@pytest.mark.parametrize("bulkcopy", PATHS, ids=PATH_IDS)
 @pytest.mark.parametrize("case", list(goldens.step_cases()), ids=lambda c: c["name"])
-def test_three_steps_both_parities(G, case, simt):
+def test_three_steps_both_parities(G, case, bulkcopy):
     """Odd, even and odd AA steps against three oracle steps (report on the even one)."""
     cfg = case["cfg"]
-    h = native_handle(cfg, simt=simt)
+    h = native_handle(cfg, bulkcopy=bulkcopy)
     put(h, case["f_in"])
     set_fields(h, case["prev"])
     fields = {k: v.astype(np.float64) for k, v in case["prev"].items()}
@@ -259,11 +259,11 @@ def test_storage_variants(G):
             assert O.weight_err(get(h, cfg.n), ref) <= tol, storage
 
 
-@pytest.mark.parametrize("simt", PATHS, ids=PATH_IDS)
+@pytest.mark.parametrize("bulkcopy", PATHS, ids=PATH_IDS)
 @pytest.mark.parametrize("lateral,vertical,obstacle", [
     ("slip", "slip", "cylinder"), ("lid", "slip", "box"), ("lid", "periodic", "sphere"),
     ("periodic", "slip", "sphere"), ("lid", "slip", "none")])
-def test_boundary_extensions(G, lateral, vertical, obstacle, simt):
+def test_boundary_extensions(G, lateral, vertical, obstacle, bulkcopy):
     """Slip z-walls and the moving lid against the oracle, obstacles touching the walls."""
     geo = {"cylinder": dict(ox=9.4, oy=6.2, r=3.1),
            "box": dict(ox=9.5, oy=9.0, oz=2.5, hx=2.5, hy=2.2, hz=4.0),
@@ -272,7 +272,7 @@ def test_boundary_extensions(G, lateral, vertical, obstacle, simt):
     cfg = O.Config(36, 11, 7, collision="les", nu=0.01, obstacle=obstacle, u0=0.06,
                    sponge_start=28.0, sponge_strength=0.8, lateral=lateral, vertical=vertical,
                    u_lid=0.05, omega_rot=0.02 if obstacle == "cylinder" else 0.0, **geo)
-    h = native_handle(cfg, simt=simt)
+    h = native_handle(cfg, bulkcopy=bulkcopy)
     assert np.array_equal(gpu_mask(h, cfg.n), O.mask(cfg).astype(np.uint8))
     h.call("lbm_init_random", 1e-3, 0.01, 7)
     f = get(h, cfg.n)
@@ -346,14 +346,15 @@ def test_nonfinite_monitors_reported(G):
 
 
 @pytest.mark.parametrize("storage,tol", [("f32", 3e-6), ("f16", 4e-4), ("bf16", 4e-3), ("f64", 1e-12)])
-def test_bulkcopy_long_rows(G, storage, tol):
+@pytest.mark.parametrize("bulkcopy", PATHS, ids=PATH_IDS)
+def test_long_rows(G, storage, tol, bulkcopy):
     """Rows of several segments (nx = 600: 256 + 256 + 88 cells), wrap-around at both
     row ends, slip walls, a rotating cylinder crossing a segment boundary; each
     storage against the oracle fed the same (storage-rounded) start state."""
     cfg = O.Config(600, 10, 6, collision="trt", nu=0.02, obstacle="cylinder", ox=255.3, oy=4.6,
                    r=3.2, u0=0.07, sponge_start=560.0, sponge_strength=0.9, lateral="slip",
                    vertical="slip", omega_rot=0.04)
-    h = native_handle(cfg, storage)
+    h = native_handle(cfg, storage, bulkcopy=bulkcopy)
     h.call("lbm_init_random", 1e-3, 0.01, 3)
     f = get(h, cfg.n)
     fields = O.new_fields(cfg.n)
