@@ -243,6 +243,22 @@ cudaError_t dispatch_export(const Ctx &c, void *dst, int dtype, cudaStream_t st)
   }
 }
 
+// Managed fields live in the GPU's HBM (the kernels write them every report
+// step) and are read by the host in place: on a coherent Grace system the CPU
+// reaches them over NVLink-C2C without migrating pages back. Advice failures
+// (systems without these attributes) leave the default placement.
+void place_on_device(void *p, size_t bytes, int device) {
+  cudaMemLocation gpu{};
+  gpu.type = cudaMemLocationTypeDevice;
+  gpu.id = device;
+  cudaMemLocation cpu{};
+  cpu.type = cudaMemLocationTypeHost;
+  cpu.id = 0;
+  if (cudaMemAdvise(p, bytes, cudaMemAdviseSetPreferredLocation, gpu) != cudaSuccess) cudaGetLastError();
+  if (cudaMemAdvise(p, bytes, cudaMemAdviseSetAccessedBy, cpu) != cudaSuccess) cudaGetLastError();
+  if (cudaMemPrefetchAsync(p, bytes, gpu, 0, 0) != cudaSuccess) cudaGetLastError();
+}
+
 void release_output(Ctx &c) {
   if (c.out_stride > 1)
     for (int k = 0; k < 5; ++k) cudaFree(c.out[k]);
@@ -429,6 +445,7 @@ lbm_status lbm_create(const lbm_config *cfg, lbm_solver **out) {
   s->bytes += (int64_t)fbytes;
   for (int k = 0; k < LBM_NUM_FIELDS; ++k) {
     e = cudaMallocManaged(&c.fld[k], (size_t)c.n * sizeof(float), cudaMemAttachGlobal);
+    if (e == cudaSuccess) place_on_device(c.fld[k], (size_t)c.n * sizeof(float), cfg->device);
     if (e == cudaSuccess) e = cudaMemset(c.fld[k], 0, (size_t)c.n * sizeof(float));
     if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("cudaMallocManaged: ") + cudaGetErrorString(e)));
     s->bytes += c.n * (int64_t)sizeof(float);
@@ -703,6 +720,7 @@ lbm_status lbm_set_output_stride(lbm_solver *s, int32_t stride) {
   for (int k = 0; k < 5; ++k) {
     c.out[k] = nullptr;
     cudaError_t e = cudaMallocManaged(&c.out[k], m * sizeof(float), cudaMemAttachGlobal);
+    if (e == cudaSuccess) place_on_device(c.out[k], m * sizeof(float), c.cfg.device);
     if (e != cudaSuccess) {
       for (int j = 0; j < k; ++j) cudaFree(c.out[j]);
       for (int j = 0; j < 5; ++j) c.out[j] = c.fld[j];
