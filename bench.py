@@ -45,9 +45,10 @@ DTYPE = {"f32": "f32", "f16": "f16 storage, f32 arithmetic", "bf16": "bf16 stora
          "f64": "f64"}
 
 
-def workload_config(storage):
+def workload_config(storage, report=False):
     w = WORKLOAD
-    return {"workload": f"LES cylinder Re 300, {w['nx']}x{w['ny']}x{w['nz']}, r 16, slip z, sponge 32",
+    return {"workload": f"LES cylinder Re 300, {w['nx']}x{w['ny']}x{w['nz']}, r 16, slip z, sponge 32"
+                        + (", report steps" if report else ""),
             "cells": w["nx"] * w["ny"] * w["nz"], "storage": storage, "collision": w["collision"],
             "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas"}
 
@@ -265,6 +266,8 @@ def main():
     ap.add_argument("--path", default="auto", choices=["auto", "simt", "bulkcopy"],
                     help="step kernel: per-cell (auto, simt) or bulk-copy staged (bulkcopy)")
     ap.add_argument("--e2e-steps", type=int, default=500)
+    ap.add_argument("--report", action="store_true",
+                    help="time report steps (13 diagnostic fields and FP64 monitor sums every step)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -283,7 +286,11 @@ def main():
     barrier(dist, torch)
     with Clocks(local) as clocks:
         t0 = time.perf_counter()
-        s.run(steps)
+        if args.report:
+            for _ in range(steps):
+                s.step(report=True)
+        else:
+            s.run(steps)
         s.sync()
         wall = time.perf_counter() - t0
     barrier(dist, torch)
@@ -296,7 +303,8 @@ def main():
     bulk_ms = t[0] / max(t[1], 1)
     kernel_name = "stream_kernel (bulk-copy)" if args.path == "bulkcopy" else "step_kernel"
     solid = int(s.mask().sum())
-    bytes_cell = BYTES_PER_CELL[args.storage]
+    # a report step also reads 4 and writes 13 float32 fields per cell (lbm.py:493-513)
+    bytes_cell = BYTES_PER_CELL[args.storage] + (68 if args.report else 0)
     # the dominant kernel updates t[2] cells (all but lid rows); its obstacle
     # cells move no bytes on a quiet step, every fluid cell moves bytes_cell
     kernel_bytes = bytes_cell * (t[2] - solid)
@@ -322,7 +330,7 @@ def main():
         "metric": "GLUPS", "value": value, "unit": "GLUPS", "n_gpus": world, "steps": steps,
         "warmup": args.warmup, "ms_per_step": span_ms / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[args.storage], "data": "synthetic",
-        "config": workload_config(args.storage),
+        "config": workload_config(args.storage, args.report),
         "e2e": {"value": e2e_value, "unit": "GLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 64,
                 "api": "Solver.step(report=True) + Solver.monitors(1) per step",
                 "ms_per_step": e2e_wall / e2e_steps * 1e3},

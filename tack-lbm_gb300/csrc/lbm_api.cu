@@ -307,14 +307,17 @@ namespace lbmh {
 
 void set_last_error(const std::string &msg) { g_err = msg; }
 
-__global__ void finalize_stage(const double *partials, int64_t nb, double *stage) {
+__global__ void finalize_stage(const float2 *partials, int64_t nb, double *stage) {
   __shared__ double sm[256][lbmk::NSUM];
   const int64_t chunk = (nb + gridDim.x - 1) / gridDim.x;
   const int64_t b0 = (int64_t)blockIdx.x * chunk;
   const int64_t b1 = b0 + chunk < nb ? b0 + chunk : nb;
   double acc[lbmk::NSUM] = {0, 0, 0, 0, 0, 0, 0, 0};
   for (int64_t b = b0 + threadIdx.x; b < b1; b += blockDim.x)
-    for (int k = 0; k < lbmk::NSUM; ++k) acc[k] += partials[b * lbmk::NSUM + k];
+    for (int k = 0; k < lbmk::NSUM; ++k) {
+      const float2 p = partials[b * lbmk::NSUM + k];
+      acc[k] += (double)p.x + (double)p.y;
+    }
   for (int k = 0; k < lbmk::NSUM; ++k) sm[threadIdx.x][k] = acc[k];
   __syncthreads();
   for (int w = 128; w > 0; w >>= 1) {
@@ -452,7 +455,7 @@ lbm_status lbm_create(const lbm_config *cfg, lbm_solver **out) {
   }
   // fast-kernel blocks plus at most one general block per four warps
   c.partial_rows = std::max<int64_t>(2 * c.nblocks + 1, (int64_t)c.num_sms * 32);
-  e = cudaMalloc(&c.partials, (size_t)c.partial_rows * lbmk::NSUM * sizeof(double));
+  e = cudaMalloc(&c.partials, (size_t)c.partial_rows * lbmk::NSUM * sizeof(float2));
   if (e == cudaSuccess) e = cudaMalloc(&c.error, sizeof(unsigned int));
   if (e == cudaSuccess) e = cudaMemset(c.error, 0, sizeof(unsigned int));
   if (e == cudaSuccess) e = cudaMalloc(&c.stage, lbmh::FINALIZE_BLOCKS * lbmk::NSUM * sizeof(double));

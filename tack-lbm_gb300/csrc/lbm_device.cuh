@@ -107,7 +107,7 @@ struct StepArgs {
   P wall_ox, wall_oy, wall_inv_r;     // cylinder axis and 1/r for the moving-wall term
   P omega_bgk, tau0, smag_c, magic;   // smag_c = 25.456 cs^2 (lbm.py:93)
   float *fld[13];
-  double *partials;       // NSUM doubles per block (report steps)
+  float2 *partials;       // NSUM compensated float pairs per block (report steps)
   int reach_lo[3], reach_hi[3];  // cells that may be solid or next to solid lie in this box
   int reach_any;                 // 0: no obstacle cell at all
   const uint32_t *masks;         // link masks of the warps in the reach box (32 words each)
@@ -409,10 +409,11 @@ __device__ __forceinline__ void sponge(T v[Q], const Moments<T> &m, T sigma, T u
 }
 
 // ---------------------------------------------------------------------------
-// Report-step sums. A float pair (Knuth's TwoSum) carries ~44 bits, so warp
-// sums of the float32 report fields lose nothing a float64 sum would keep; the
-// warps' pairs are then added in float64 (GB300's float64 pipe is narrow, so
-// float64 is kept to a handful of operations per block).
+// Report-step sums. A float pair (Knuth's TwoSum) carries ~44 bits, so the
+// warp and block sums of the float32 report fields lose nothing a float64 sum
+// would keep. GB300's float64 pipe is narrow (a warp instruction costs many
+// cycles whatever its active lanes), so the step kernels use no float64 at
+// all: the pairs are added in float64 by the finalize kernel only.
 
 struct CSum {
   float hi, lo;
@@ -436,20 +437,22 @@ __device__ __forceinline__ CSum warp_csum(float v) {
   return x;
 }
 
-__device__ __forceinline__ void block_sums(const float v[NSUM], double *partials, int bid) {
-  __shared__ double red[BY][NSUM];
+// Each block writes its 8 sums as compensated float pairs (hi, lo); only the
+// finalize kernel converts them to float64.
+__device__ __forceinline__ void block_sums(const float v[NSUM], float2 *partials, int bid) {
+  __shared__ CSum red[BY][NSUM];
   const int lane = threadIdx.x, warp = threadIdx.y;
 #pragma unroll
   for (int k = 0; k < NSUM; ++k) {
     const CSum s = warp_csum(v[k]);
-    if (lane == 0) red[warp][k] = (double)s.hi + (double)s.lo;
+    if (lane == 0) red[warp][k] = s;
   }
   __syncthreads();
   if (warp == 0 && lane < NSUM) {
-    double s = 0.0;
+    CSum s = red[0][lane];
 #pragma unroll
-    for (int w = 0; w < BY; ++w) s += red[w][lane];
-    partials[(size_t)bid * NSUM + lane] = s;
+    for (int w = 1; w < BY; ++w) s = csum_add(s, red[w][lane]);
+    partials[(size_t)bid * NSUM + lane] = make_float2(s.hi, s.lo);
   }
 }
 
@@ -459,7 +462,7 @@ __device__ __forceinline__ void diagnostics(float *const fld[13], int idx, const
                                             float mx, float my, float mz, float v[NSUM]) {
   const float rho = (float)m.rho;
   const float ux = (float)m.ux, uy = (float)m.uy, uz = (float)m.uz;
-  const float p = (float)(m.drho / T(3));
+  const float p = (float)(m.drho * T(1.0 / 3.0));
   const float ke = 0.5f * rho * (ux * ux + uy * uy + uz * uz);
   const float ox = fld[0][idx], oy = fld[1][idx], oz = fld[2][idx], op = fld[3][idx];
   const float ok = 0.5f * (ox * ox + oy * oy + oz * oz);

@@ -349,7 +349,7 @@ __global__ void __launch_bounds__(SW + 32) stream_kernel(const __grid_constant__
   S *stages = reinterpret_cast<S *>(smem_raw);
   uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + (size_t)NST * L::STAGE * sizeof(S));
   uint64_t *empty = full + NST;
-  __shared__ double red[SW / 32][NSUM];
+  __shared__ CSum red[SW / 32][NSUM];
   __shared__ DirTab tab[Q];
   __shared__ SegInfo info[L::NST];
   const int tid = threadIdx.x;
@@ -434,12 +434,12 @@ __global__ void __launch_bounds__(SW + 32) stream_kernel(const __grid_constant__
   }
   if (REPORT) {
     if (lane == 0)
-      for (int k = 0; k < NSUM; ++k) red[warp][k] = (double)acc[k].hi + (double)acc[k].lo;
+      for (int k = 0; k < NSUM; ++k) red[warp][k] = acc[k];
     consumer_sync();
     if (tid < NSUM) {
-      double s = 0.0;
-      for (int w = 0; w < SW / 32; ++w) s += red[w][tid];
-      sa.a.partials[(size_t)blockIdx.x * NSUM + tid] = s;
+      CSum s = red[0][tid];
+      for (int w = 1; w < SW / 32; ++w) s = csum_add(s, red[w][tid]);
+      sa.a.partials[(size_t)blockIdx.x * NSUM + tid] = make_float2(s.hi, s.lo);
     }
   }
 }
