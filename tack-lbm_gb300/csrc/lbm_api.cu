@@ -288,6 +288,7 @@ void release(lbm_solver *s) {
   cudaFree(c.error);
   cudaFree(c.special);
   cudaFree(c.wmasks);
+  cudaFree(c.fld_dev);
   if (c.side) cudaStreamDestroy(c.side);
   if (c.fork) cudaEventDestroy(c.fork);
   if (c.join) cudaEventDestroy(c.join);
@@ -455,6 +456,9 @@ lbm_status lbm_create(const lbm_config *cfg, lbm_solver **out) {
   }
   // fast-kernel blocks plus at most one general block per four warps
   c.partial_rows = std::max<int64_t>(2 * c.nblocks + 1, (int64_t)c.num_sms * 32);
+  e = cudaMalloc(&c.fld_dev, LBM_NUM_FIELDS * sizeof(float *));
+  if (e == cudaSuccess) e = cudaMemcpy(c.fld_dev, c.fld, LBM_NUM_FIELDS * sizeof(float *), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("field table: ") + cudaGetErrorString(e)));
   e = cudaMalloc(&c.partials, (size_t)c.partial_rows * lbmk::NSUM * sizeof(float2));
   if (e == cudaSuccess) e = cudaMalloc(&c.error, sizeof(unsigned int));
   if (e == cudaSuccess) e = cudaMemset(c.error, 0, sizeof(unsigned int));

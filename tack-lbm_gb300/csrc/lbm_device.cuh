@@ -437,26 +437,45 @@ __device__ __forceinline__ CSum warp_csum(float v) {
   return x;
 }
 
-// Each block writes its 8 sums as compensated float pairs (hi, lo); only the
-// finalize kernel converts them to float64.
-__device__ __forceinline__ void block_sums(const float v[NSUM], float2 *partials, int bid) {
-  __shared__ CSum red[BY][NSUM];
-  const int lane = threadIdx.x, warp = threadIdx.y;
+// Monitor sums of a report step: the 8 summed fields (r_rho, r_ux, r_uy, r_uz,
+// r_ke, fx, fy, fz) are read back once by a streaming kernel. Each thread keeps
+// compensated float pairs over its cells, then warp and block pairs; every
+// block writes 8 pairs and only the finalize kernel works in float64.
+constexpr int SUM_THREADS = 256;
+
+static __global__ void __launch_bounds__(SUM_THREADS) field_sums_kernel(const float *const *fld, int n, float2 *partials) {
+  __shared__ CSum red[SUM_THREADS / 32][NSUM];
+  CSum acc[NSUM];
+#pragma unroll
+  for (int k = 0; k < NSUM; ++k) acc[k] = {0.f, 0.f};
+  const float *f[NSUM];
+#pragma unroll
+  for (int k = 0; k < NSUM; ++k) f[k] = fld[5 + k];
+  for (int i = blockIdx.x * SUM_THREADS + threadIdx.x; i < n; i += gridDim.x * SUM_THREADS) {
+#pragma unroll
+    for (int k = 0; k < NSUM; ++k) acc[k] = csum_add(acc[k], CSum{f[k][i], 0.f});
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < NSUM; ++k) {
-    const CSum s = warp_csum(v[k]);
-    if (lane == 0) red[warp][k] = s;
+    CSum x = acc[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      CSum y{__shfl_down_sync(0xffffffffu, x.hi, o), __shfl_down_sync(0xffffffffu, x.lo, o)};
+      x = csum_add(x, y);
+    }
+    if (lane == 0) red[warp][k] = x;
   }
   __syncthreads();
-  if (warp == 0 && lane < NSUM) {
-    CSum s = red[0][lane];
-#pragma unroll
-    for (int w = 1; w < BY; ++w) s = csum_add(s, red[w][lane]);
-    partials[(size_t)bid * NSUM + lane] = make_float2(s.hi, s.lo);
+  if (threadIdx.x < NSUM) {
+    CSum s = red[0][threadIdx.x];
+    for (int w = 1; w < SUM_THREADS / 32; ++w) s = csum_add(s, red[w][threadIdx.x]);
+    partials[(size_t)blockIdx.x * NSUM + threadIdx.x] = make_float2(s.hi, s.lo);
   }
 }
 
-// Diagnostics of one cell (lbm.py:493-513); the values monitors() sums are added to v[].
+// Diagnostics of one cell (lbm.py:493-513). v[] collects the summed values
+// (the bulk-copy kernel reduces them itself).
 template <typename T>
 __device__ __forceinline__ void diagnostics(float *const fld[13], int idx, const Moments<T> &m,
                                             float mx, float my, float mz, float v[NSUM]) {
@@ -795,7 +814,6 @@ step_kernel(const __grid_constant__ StepArgs<S> a) {
       }
     }
   }
-  if (REPORT) block_sums(v, a.partials, block_id());
 }
 
 // Link masks of the warps within the obstacle's reach, one warp per 32 cells.
@@ -834,7 +852,7 @@ general_kernel(const __grid_constant__ StepArgs<S> a, const int *list, int count
     if (x < a.nx)
       general_cell<S, COLL, REPORT, ODD>(a, x, y, z, (z * a.ny + y) * a.nx + x, mask_slot(a, x0, y, z) >= 0, v);
   }
-  if (REPORT) block_sums(v, a.partials, row0 + (int)blockIdx.x);
+  (void)row0;
 }
 
 // ---------------------------------------------------------------------------

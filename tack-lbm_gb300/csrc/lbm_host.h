@@ -16,6 +16,7 @@ struct Ctx {
   int64_t n;                 // cells
   void *F;                   // 19*n populations, storage precision cfg.storage
   float *fld[LBM_NUM_FIELDS];
+  float **fld_dev;           // the field pointers in device memory (for the sums kernel)
   float2 *partials;          // 8 compensated float pairs per block (report steps)
   double *stage;             // finalize stage: 8 doubles per finalize block
   double *sums;              // 8 doubles: the last report step's FP64 sums

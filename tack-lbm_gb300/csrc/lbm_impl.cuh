@@ -5,6 +5,8 @@
 #include "lbm_host.h"
 #include "lbm_stream.cuh"
 
+#include <algorithm>
+
 namespace lbmh {
 
 using namespace lbmk;
@@ -98,7 +100,15 @@ cudaError_t launch_variant(const Ctx &c, const StepArgs<S> &a, cudaStream_t st, 
     step_kernel<S, COLL, REPORT, ODD><<<grid, block, 0, st>>>(a);
     if (ev) cudaEventRecord(ev[1], st);
     if (gblocks > 0) cudaStreamWaitEvent(st, c.join, 0);
-    *rows = fblocks + gblocks;
+    *rows = 0;
+    if (REPORT) {
+      // the monitor sums, read back from the fields just written
+      const int sblocks = (int)std::min<int64_t>((c.n + SUM_THREADS * 16 - 1) / (SUM_THREADS * 16),
+                                                 (int64_t)c.num_sms * 8);
+      field_sums_kernel<<<sblocks, SUM_THREADS, 0, st>>>(c.fld_dev, (int)c.n, c.partials);
+      *rows = sblocks;
+    }
+    (void)fblocks;
   }
   if (ev) cudaEventRecord(ev[2], st);
   return cudaGetLastError();
