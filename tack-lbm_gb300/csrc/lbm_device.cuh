@@ -474,19 +474,29 @@ static __global__ void __launch_bounds__(SUM_THREADS) field_sums_kernel(const fl
   }
 }
 
+// The previous report's ux, uy, uz, p of a cell. Report steps load them with
+// the populations, before any store: the field and population pointers may
+// alias as far as the compiler knows, so a load issued after the stores would
+// add a second, unhidden memory round trip to every cell.
+struct Prev {
+  float ux, uy, uz, p;
+};
+__device__ __forceinline__ Prev load_prev(float *const fld[13], int idx) {
+  return Prev{fld[0][idx], fld[1][idx], fld[2][idx], fld[3][idx]};
+}
+
 // Diagnostics of one cell (lbm.py:493-513). v[] collects the summed values
 // (the bulk-copy kernel reduces them itself).
 template <typename T>
-__device__ __forceinline__ void diagnostics(float *const fld[13], int idx, const Moments<T> &m,
-                                            float mx, float my, float mz, float v[NSUM]) {
+__device__ __forceinline__ void diagnostics(float *const fld[13], int idx, const Moments<T> &m, float mx,
+                                            float my, float mz, const Prev &o, float v[NSUM]) {
   const float rho = (float)m.rho;
   const float ux = (float)m.ux, uy = (float)m.uy, uz = (float)m.uz;
   const float p = (float)(m.drho * T(1.0 / 3.0));
   const float ke = 0.5f * rho * (ux * ux + uy * uy + uz * uz);
-  const float ox = fld[0][idx], oy = fld[1][idx], oz = fld[2][idx], op = fld[3][idx];
-  const float ok = 0.5f * (ox * ox + oy * oy + oz * oz);
-  const float dp = 3.0f * (p - op);
-  const float r[5] = {dp * dp, (ux - ox) * (ux - ox), (uy - oy) * (uy - oy), (uz - oz) * (uz - oz),
+  const float ok = 0.5f * (o.ux * o.ux + o.uy * o.uy + o.uz * o.uz);
+  const float dp = 3.0f * (p - o.p);
+  const float r[5] = {dp * dp, (ux - o.ux) * (ux - o.ux), (uy - o.uy) * (uy - o.uy), (uz - o.uz) * (uz - o.uz),
                       (ke - ok) * (ke - ok)};
 #pragma unroll
   for (int k = 0; k < 5; ++k) v[k] += r[k];
@@ -587,6 +597,7 @@ __device__ __forceinline__ typename Store<S>::T wall_term(const StepArgs<S> &a, 
 template <typename S, bool ODD, bool SPECIAL>
 __device__ __forceinline__ void fast_load(const StepArgs<S> &a, int idx, const Offsets<S> &o, const Row &r,
                                           uint32_t m, typename Store<S>::T d[Q]) {
+  // (report steps load the previous fields beside this, see load_prev)
   static_for<Q>([&](auto qc) {
     constexpr int q = decltype(qc)::value;
     S *own = a.slot[q] + idx;
@@ -604,7 +615,8 @@ __device__ __forceinline__ void fast_load(const StepArgs<S> &a, int idx, const O
 
 template <typename S, int COLL, bool REPORT, bool ODD, bool SPECIAL>
 __device__ __forceinline__ void fast_finish(const StepArgs<S> &a, int x, int y, int idx, const Offsets<S> &o,
-                                            const Row &r, uint32_t m, typename Store<S>::T d[Q], float v[NSUM]) {
+                                            const Row &r, uint32_t m, typename Store<S>::T d[Q], const Prev &prev,
+                                            float v[NSUM]) {
   using T = typename Store<S>::T;
   constexpr bool DEV = Store<S>::DEV;
   const bool here = SPECIAL && (m & MASK_SOLID);
@@ -643,7 +655,7 @@ __device__ __forceinline__ void fast_finish(const StepArgs<S> &a, int x, int y, 
       else Store<S>::template store<p>(a.slot[opp(p)] + idx, d[p]);
     });
   }
-  if (REPORT) diagnostics<T>(a.fld, idx, mo, mx, my, mz, v);
+  if (REPORT) diagnostics<T>(a.fld, idx, mo, mx, my, mz, prev, v);
 }
 
 template <typename S>
@@ -713,6 +725,8 @@ __device__ __forceinline__ void general_cell(const StepArgs<S> &a, int x, int y,
   constexpr bool DEV = Store<S>::DEV;
   const bool here = geo && solid(a.geo, x, y, z);
   if (here && !REPORT) return;
+  Prev prev{0.f, 0.f, 0.f, 0.f};
+  if (REPORT) prev = load_prev(a.fld, idx);
   T d[Q];
   float mx = 0.f, my = 0.f, mz = 0.f;
   static_for<Q>([&](auto qc) {
@@ -761,7 +775,7 @@ __device__ __forceinline__ void general_cell(const StepArgs<S> &a, int x, int y,
       Store<S>::template store<p>(dst, d[p]);
     });
   }
-  if (REPORT) diagnostics<T>(a.fld, idx, m, mx, my, mz, v);
+  if (REPORT) diagnostics<T>(a.fld, idx, m, mx, my, mz, prev, v);
 }
 
 // A warp is one row segment of 32 cells, so every choice below is uniform per warp.
@@ -803,14 +817,17 @@ step_kernel(const __grid_constant__ StepArgs<S> a) {
     const int ms = mask_slot(a, x0, y, z);
     const Offsets<S> o = cell_offsets(a, x, y, z);
     T d[Q];
+    Prev prev{0.f, 0.f, 0.f, 0.f};
     if (!(r.ylo || r.yhi || r.zlo || r.zhi) && ms < 0) {
+      if (REPORT) prev = load_prev(a.fld, idx);
       fast_load<S, ODD, false>(a, idx, o, r, 0u, d);
-      fast_finish<S, COLL, REPORT, ODD, false>(a, x, y, idx, o, r, 0u, d, v);
+      fast_finish<S, COLL, REPORT, ODD, false>(a, x, y, idx, o, r, 0u, d, prev, v);
     } else {
       const uint32_t m = ms >= 0 ? a.masks[ms + (int)threadIdx.x] : 0u;
       if (REPORT || !(m & MASK_SOLID)) {
+        if (REPORT) prev = load_prev(a.fld, idx);
         fast_load<S, ODD, true>(a, idx, o, r, m, d);
-        fast_finish<S, COLL, REPORT, ODD, true>(a, x, y, idx, o, r, m, d, v);
+        fast_finish<S, COLL, REPORT, ODD, true>(a, x, y, idx, o, r, m, d, prev, v);
       }
     }
   }

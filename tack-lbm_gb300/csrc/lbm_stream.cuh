@@ -272,6 +272,8 @@ __device__ __forceinline__ void stream_cell(const StepArgs<S> &a, const SegInfo 
   if (here && !REPORT) return;
   const int x = g.x0 + i;
   const int idx = (g.z * a.ny + g.y) * a.nx + x;
+  Prev prev{0.f, 0.f, 0.f, 0.f};
+  if (REPORT) prev = load_prev(a.fld, idx);
   // buffer element of population q for this cell (the lid row's y-bounced pieces are unshifted)
   auto pos = [&](auto qc) {
     constexpr int q = decltype(qc)::value;
@@ -322,7 +324,7 @@ __device__ __forceinline__ void stream_cell(const StepArgs<S> &a, const SegInfo 
       Store<S>::template store<p>(stage + pos(std::integral_constant<int, opp(p)>{}), d[p]);
     });
   }
-  if (REPORT) diagnostics<T>(a.fld, idx, mo, mx, my, mz, v);
+  if (REPORT) diagnostics<T>(a.fld, idx, mo, mx, my, mz, prev, v);
 }
 
 __device__ __forceinline__ bool wait_phase(uint64_t *bar, uint32_t parity) {
