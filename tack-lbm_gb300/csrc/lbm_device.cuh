@@ -331,6 +331,23 @@ __device__ __forceinline__ T rv_of(const Moments<T> &m) {
   return DEV ? m.drho : m.rho;
 }
 
+// v <- v + om (feq - v), written v (1 - om) + om feq: with om w A and om w B
+// formed once per pair that is one fused multiply-add per population.
+template <typename T>
+__device__ __forceinline__ void relax_bgk(T v[Q], T om, const T A[9], const T B[9], T eq0) {
+  const T keep = T(1) - om;
+  const T om1 = om * T(wq(1)), om7 = om * T(wq(7));
+  v[0] = v[0] * keep + om * eq0;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    const int q = pq(k);
+    const T ow = k < 3 ? om1 : om7;
+    const T oA = ow * A[k], oB = ow * B[k];
+    v[q] = v[q] * keep + (oA + oB);
+    v[q + 1] = v[q + 1] * keep + (oA - oB);
+  }
+}
+
 // Relax the values v[] in place: BGK (lbm.py:60-69), TRT + Smagorinsky
 // (lbm.py:96-123), LES-BGK (lbm.py:126-139).
 template <typename T, int COLL, bool DEV>
@@ -339,14 +356,7 @@ __device__ __forceinline__ void collide(T v[Q], const Moments<T> &m, const Pairs
   T A[9], B[9], eq0;
   eq_pairs<T, DEV>(rv_of<T, DEV>(m), m.rho, m.ux, m.uy, m.uz, A, B, eq0);
   if (COLL == COLL_BGK) {
-    v[0] += omega_bgk * (eq0 - v[0]);
-#pragma unroll
-    for (int k = 0; k < 9; ++k) {
-      const int q = pq(k);
-      const T wA = T(wq(q)) * A[k], wB = T(wq(q)) * B[k];
-      v[q] += omega_bgk * ((wA + wB) - v[q]);
-      v[q + 1] += omega_bgk * ((wA - wB) - v[q + 1]);
-    }
+    relax_bgk<T>(v, omega_bgk, A, B, eq0);
     return;
   }
   // Smagorinsky relaxation time from the non-equilibrium stress (lbm.py:72-93)
@@ -364,15 +374,7 @@ __device__ __forceinline__ void collide(T v[Q], const Moments<T> &m, const Pairs
   const T pi = sqrt_fast<T>(pxx * pxx + pyy * pyy + pzz * pzz + T(2) * (pxy * pxy + pxz * pxz + pyz * pyz));
   const T tau = T(0.5) * (tau0 + sqrt_fast<T>(tau0 * tau0 + smag_c * pi * rcp_fast<T>(m.rho)));
   if (COLL == COLL_LES) {
-    const T om = rcp_fast<T>(tau);
-    v[0] += om * (eq0 - v[0]);
-#pragma unroll
-    for (int k = 0; k < 9; ++k) {
-      const int q = pq(k);
-      const T wA = T(wq(q)) * A[k], wB = T(wq(q)) * B[k];
-      v[q] += om * ((wA + wB) - v[q]);
-      v[q + 1] += om * ((wA - wB) - v[q + 1]);
-    }
+    relax_bgk<T>(v, rcp_fast<T>(tau), A, B, eq0);
     return;
   }
   // TRT: even/odd parts relaxed at omega+ = 1/tau, omega- = 1/(magic/(tau-1/2)+1/2)
@@ -802,14 +804,10 @@ __device__ __forceinline__ bool lid_row(const StepArgs<S> &a, int y) {
 #define LBM_STEP_MIN_BLOCKS 5
 #endif
 
+// One cell of the per-cell kernels: the warp is the 32-cell row segment at x0.
 template <typename S, int COLL, bool REPORT, bool ODD>
-__global__ void __launch_bounds__(BX * BY, LBM_STEP_MIN_BLOCKS)
-step_kernel(const __grid_constant__ StepArgs<S> a) {
+__device__ __forceinline__ void cell_step(const StepArgs<S> &a, int x0, int x, int y, int z) {
   using T = typename Store<S>::T;
-  const int x0 = (int)blockIdx.x * BX;
-  const int x = x0 + (int)threadIdx.x;
-  const int y = (int)blockIdx.y * BY + (int)threadIdx.y;
-  const int z = (int)blockIdx.z;
   float v[NSUM] = {0, 0, 0, 0, 0, 0, 0, 0};
   if (y < a.ny && !lid_row(a, y) && x < a.nx) {
     const int idx = (z * a.ny + y) * a.nx + x;
@@ -831,6 +829,14 @@ step_kernel(const __grid_constant__ StepArgs<S> a) {
       }
     }
   }
+}
+
+template <typename S, int COLL, bool REPORT, bool ODD>
+__global__ void __launch_bounds__(BX * BY, LBM_STEP_MIN_BLOCKS)
+step_kernel(const __grid_constant__ StepArgs<S> a) {
+  const int x0 = (int)blockIdx.x * BX;
+  cell_step<S, COLL, REPORT, ODD>(a, x0, x0 + (int)threadIdx.x, (int)blockIdx.y * BY + (int)threadIdx.y,
+                                  (int)blockIdx.z);
 }
 
 // Link masks of the warps within the obstacle's reach, one warp per 32 cells.

@@ -17,6 +17,7 @@ import pytest
 
 from oracle import lbm_oracle as O
 import goldens
+import lbm_native as N
 
 pytestmark = pytest.mark.gpu
 
@@ -31,11 +32,10 @@ def G():
     return G
 
 
-def native_handle(cfg, storage="f32", bulkcopy=False):
-    """A solver for cfg; bulkcopy=True selects the bulk-copy (TMA) staged step kernel."""
-    import lbm_native as N
+def native_handle(cfg, storage="f32", flags=0):
+    """A solver for cfg; flags (LBM_FLAG_*) picks the step kernel."""
     c = N.Config()
-    c.flags = N.FLAG_BULKCOPY if bulkcopy else 0
+    c.flags = flags
     c.nx, c.ny, c.nz = cfg.nx, cfg.ny, cfg.nz
     c.collision = N.COLLISION[cfg.collision]
     c.obstacle = N.OBSTACLE[cfg.obstacle]
@@ -125,15 +125,16 @@ def test_trt_ref_through_kernel_entry(G):
     assert O.weight_err(out, z["ref"]) <= 2e-6           # trt_ref uses exact weights
 
 
-PATHS = [False, True]
+# step kernels: the per-cell kernel (default) and the bulk-copy staged kernel
+PATHS = [0, N.FLAG_BULKCOPY]
 PATH_IDS = ["percell", "bulkcopy"]
 
 
-@pytest.mark.parametrize("bulkcopy", PATHS, ids=PATH_IDS)
+@pytest.mark.parametrize("kernel", PATHS, ids=PATH_IDS)
 @pytest.mark.parametrize("case", list(goldens.step_cases()), ids=lambda c: c["name"])
-def test_golden_step(G, case, bulkcopy):
+def test_golden_step(G, case, kernel):
     cfg = case["cfg"]
-    h = native_handle(cfg, bulkcopy=bulkcopy)
+    h = native_handle(cfg, flags=kernel)
     assert np.array_equal(gpu_mask(h, cfg.n), case["solid"])
     put(h, case["f_in"])
     set_fields(h, case["prev"])
@@ -144,12 +145,12 @@ def test_golden_step(G, case, bulkcopy):
         check_fields(get_fields(h, cfg.n), case["fields"], case["name"])
 
 
-@pytest.mark.parametrize("bulkcopy", PATHS, ids=PATH_IDS)
+@pytest.mark.parametrize("kernel", PATHS, ids=PATH_IDS)
 @pytest.mark.parametrize("case", list(goldens.step_cases()), ids=lambda c: c["name"])
-def test_three_steps_both_parities(G, case, bulkcopy):
+def test_three_steps_both_parities(G, case, kernel):
     """Odd, even and odd AA steps against three oracle steps (report on the even one)."""
     cfg = case["cfg"]
-    h = native_handle(cfg, bulkcopy=bulkcopy)
+    h = native_handle(cfg, flags=kernel)
     put(h, case["f_in"])
     set_fields(h, case["prev"])
     fields = {k: v.astype(np.float64) for k, v in case["prev"].items()}
@@ -259,11 +260,11 @@ def test_storage_variants(G):
             assert O.weight_err(get(h, cfg.n), ref) <= tol, storage
 
 
-@pytest.mark.parametrize("bulkcopy", PATHS, ids=PATH_IDS)
+@pytest.mark.parametrize("kernel", PATHS, ids=PATH_IDS)
 @pytest.mark.parametrize("lateral,vertical,obstacle", [
     ("slip", "slip", "cylinder"), ("lid", "slip", "box"), ("lid", "periodic", "sphere"),
     ("periodic", "slip", "sphere"), ("lid", "slip", "none")])
-def test_boundary_extensions(G, lateral, vertical, obstacle, bulkcopy):
+def test_boundary_extensions(G, lateral, vertical, obstacle, kernel):
     """Slip z-walls and the moving lid against the oracle, obstacles touching the walls."""
     geo = {"cylinder": dict(ox=9.4, oy=6.2, r=3.1),
            "box": dict(ox=9.5, oy=9.0, oz=2.5, hx=2.5, hy=2.2, hz=4.0),
@@ -272,7 +273,7 @@ def test_boundary_extensions(G, lateral, vertical, obstacle, bulkcopy):
     cfg = O.Config(36, 11, 7, collision="les", nu=0.01, obstacle=obstacle, u0=0.06,
                    sponge_start=28.0, sponge_strength=0.8, lateral=lateral, vertical=vertical,
                    u_lid=0.05, omega_rot=0.02 if obstacle == "cylinder" else 0.0, **geo)
-    h = native_handle(cfg, bulkcopy=bulkcopy)
+    h = native_handle(cfg, flags=kernel)
     assert np.array_equal(gpu_mask(h, cfg.n), O.mask(cfg).astype(np.uint8))
     h.call("lbm_init_random", 1e-3, 0.01, 7)
     f = get(h, cfg.n)
@@ -346,15 +347,15 @@ def test_nonfinite_monitors_reported(G):
 
 
 @pytest.mark.parametrize("storage,tol", [("f32", 3e-6), ("f16", 4e-4), ("bf16", 4e-3), ("f64", 1e-12)])
-@pytest.mark.parametrize("bulkcopy", PATHS, ids=PATH_IDS)
-def test_long_rows(G, storage, tol, bulkcopy):
+@pytest.mark.parametrize("kernel", PATHS, ids=PATH_IDS)
+def test_long_rows(G, storage, tol, kernel):
     """Rows of several segments (nx = 600: 256 + 256 + 88 cells), wrap-around at both
     row ends, slip walls, a rotating cylinder crossing a segment boundary; each
     storage against the oracle fed the same (storage-rounded) start state."""
     cfg = O.Config(600, 10, 6, collision="trt", nu=0.02, obstacle="cylinder", ox=255.3, oy=4.6,
                    r=3.2, u0=0.07, sponge_start=560.0, sponge_strength=0.9, lateral="slip",
                    vertical="slip", omega_rot=0.04)
-    h = native_handle(cfg, storage, bulkcopy=bulkcopy)
+    h = native_handle(cfg, storage, flags=kernel)
     h.call("lbm_init_random", 1e-3, 0.01, 3)
     f = get(h, cfg.n)
     fields = O.new_fields(cfg.n)
