@@ -286,6 +286,7 @@ void release(lbm_solver *s) {
   cudaFree(c.seg_list);
   cudaFree(c.masks);
   cudaFree(c.error);
+  cudaFree(c.ticket);
   cudaFree(c.special);
   cudaFree(c.wmasks);
   cudaFree(c.fld_dev);
@@ -462,6 +463,8 @@ lbm_status lbm_create(const lbm_config *cfg, lbm_solver **out) {
   e = cudaMalloc(&c.partials, (size_t)c.partial_rows * lbmk::NSUM * sizeof(float2));
   if (e == cudaSuccess) e = cudaMalloc(&c.error, sizeof(unsigned int));
   if (e == cudaSuccess) e = cudaMemset(c.error, 0, sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMalloc(&c.ticket, sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMemset(c.ticket, 0, sizeof(unsigned int));
   if (e == cudaSuccess) e = cudaMalloc(&c.stage, lbmh::FINALIZE_BLOCKS * lbmk::NSUM * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&c.sums, lbmk::NSUM * sizeof(double));
   if (e == cudaSuccess) e = cudaMemset(c.sums, 0, lbmk::NSUM * sizeof(double));

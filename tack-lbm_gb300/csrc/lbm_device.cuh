@@ -440,20 +440,45 @@ __device__ __forceinline__ CSum warp_csum(float v) {
 }
 
 // Monitor sums of a report step: the 8 summed fields (r_rho, r_ux, r_uy, r_uz,
-// r_ke, fx, fy, fz) are read back once by a streaming kernel. Each thread keeps
-// compensated float pairs over its cells, then warp and block pairs; every
-// block writes 8 pairs and only the finalize kernel works in float64.
+// r_ke, fx, fy, fz) are read back once by a streaming kernel, four cells per
+// load when n % 4 == 0. Each thread keeps compensated float pairs over its
+// cells, then warp and block pairs; every block writes 8 pairs. The last block
+// to finish (an atomic ticket, no waiting) adds the blocks' pairs in float64,
+// writes the 8 sums and resets the ticket for the next report step.
 constexpr int SUM_THREADS = 256;
 
-static __global__ void __launch_bounds__(SUM_THREADS) field_sums_kernel(const float *const *fld, int n, float2 *partials) {
+__device__ __forceinline__ void csum4(CSum &acc, float4 v) {
+  acc = csum_add(acc, CSum{v.x, 0.f});
+  acc = csum_add(acc, CSum{v.y, 0.f});
+  acc = csum_add(acc, CSum{v.z, 0.f});
+  acc = csum_add(acc, CSum{v.w, 0.f});
+}
+
+static __global__ void __launch_bounds__(SUM_THREADS)
+field_sums_kernel(const float *const *fld, int n, float2 *partials, unsigned int *ticket, double *sums) {
   __shared__ CSum red[SUM_THREADS / 32][NSUM];
+  __shared__ double fin[SUM_THREADS / 32][NSUM];
+  __shared__ bool last;
   CSum acc[NSUM];
 #pragma unroll
   for (int k = 0; k < NSUM; ++k) acc[k] = {0.f, 0.f};
   const float *f[NSUM];
 #pragma unroll
   for (int k = 0; k < NSUM; ++k) f[k] = fld[5 + k];
-  for (int i = blockIdx.x * SUM_THREADS + threadIdx.x; i < n; i += gridDim.x * SUM_THREADS) {
+  const int stride = (int)gridDim.x * SUM_THREADS;
+  int tail = 0;
+  if ((n & 3) == 0) {
+    const int n4 = n >> 2;
+    for (int i = (int)blockIdx.x * SUM_THREADS + (int)threadIdx.x; i < n4; i += stride) {
+      float4 v[NSUM];
+#pragma unroll
+      for (int k = 0; k < NSUM; ++k) v[k] = reinterpret_cast<const float4 *>(f[k])[i];
+#pragma unroll
+      for (int k = 0; k < NSUM; ++k) csum4(acc[k], v[k]);
+    }
+    tail = n;
+  }
+  for (int i = tail + (int)blockIdx.x * SUM_THREADS + (int)threadIdx.x; i < n; i += stride) {
 #pragma unroll
     for (int k = 0; k < NSUM; ++k) acc[k] = csum_add(acc[k], CSum{f[k][i], 0.f});
   }
@@ -473,7 +498,35 @@ static __global__ void __launch_bounds__(SUM_THREADS) field_sums_kernel(const fl
     CSum s = red[0][threadIdx.x];
     for (int w = 1; w < SUM_THREADS / 32; ++w) s = csum_add(s, red[w][threadIdx.x]);
     partials[(size_t)blockIdx.x * NSUM + threadIdx.x] = make_float2(s.hi, s.lo);
+    __threadfence();
   }
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double d[NSUM] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += SUM_THREADS) {
+#pragma unroll
+    for (int k = 0; k < NSUM; ++k) {
+      const float2 p = __ldcg(&partials[(size_t)b * NSUM + k]);
+      d[k] += (double)p.x + (double)p.y;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < NSUM; ++k) {
+    double x = d[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) fin[warp][k] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < NSUM) {
+    double x = 0.0;
+    for (int w = 0; w < SUM_THREADS / 32; ++w) x += fin[w][threadIdx.x];
+    sums[threadIdx.x] = x;
+  }
+  if (threadIdx.x == 0) *ticket = 0u;
 }
 
 // The previous report's ux, uy, uz, p of a cell. Report steps load them with

@@ -105,8 +105,8 @@ cudaError_t launch_variant(const Ctx &c, const StepArgs<S> &a, cudaStream_t st, 
       // the monitor sums, read back from the fields just written
       const int sblocks = (int)std::min<int64_t>((c.n + SUM_THREADS * 16 - 1) / (SUM_THREADS * 16),
                                                  (int64_t)c.num_sms * 8);
-      field_sums_kernel<<<sblocks, SUM_THREADS, 0, st>>>(c.fld_dev, (int)c.n, c.partials);
-      *rows = sblocks;
+      field_sums_kernel<<<sblocks, SUM_THREADS, 0, st>>>(c.fld_dev, (int)c.n, c.partials, c.ticket, c.sums);
+      *rows = 0;  // finalized by the kernel's last block
     }
     (void)fblocks;
   }
@@ -133,7 +133,7 @@ cudaError_t launch_step(const Ctx &c, bool report, cudaStream_t st) {
     default: e = launch_coll<S, COLL_LES>(c, a, report, st, &rows); break;
   }
   if (e != cudaSuccess) return e;
-  return report ? launch_finalize(c, rows, st) : cudaSuccess;
+  return report && rows > 0 ? launch_finalize(c, rows, st) : cudaSuccess;
 }
 
 template <typename S>
