@@ -41,6 +41,11 @@ WORKLOAD = dict(nx=512, ny=256, nz=64, collision="les", reynolds=300.0, u0=0.08,
                 obstacle="cylinder", center=(128.0, 128.0, 32.0), vertical="slip", lateral="periodic",
                 sponge_planes=32, u_noise=1e-3, rho_sigma=0.0, seed=20240601)
 BYTES_PER_CELL = {"f32": 152, "f16": 76, "bf16": 76, "f64": 304}
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one step_kernel
+# launch of this workload, the mean of the two launches (even, odd) of one ncu
+# capture: profiles/step_kernel_les_cylinder_512x256x64_f32.md,
+# ..._f16.md and step_kernel_report_les_cylinder_512x256x64_f32.md.
+NCU_TRAFFIC = {("f32", False): 1214.0e6, ("f16", False): 582.5e6, ("f32", True): 1783.4e6}
 DTYPE = {"f32": "f32", "f16": "f16 storage, f32 arithmetic", "bf16": "bf16 storage, f32 arithmetic",
          "f64": "f64"}
 
@@ -336,7 +341,10 @@ def main():
                 "ms_per_step": e2e_wall / e2e_steps * 1e3},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs (burst copy)",
-                     "traffic": None, "kernel": kernel_name, "bytes_per_cell": bytes_cell,
+                     "traffic": (NCU_TRAFFIC.get((args.storage, bool(args.report)))
+                                 if args.path != "bulkcopy" else None),
+                     "traffic_unit": "B per launch (ncu dram read + write)",
+                     "kernel": kernel_name, "bytes_per_cell": bytes_cell,
                      "fluid_cells_per_launch": int(t[2] - solid), "ms_per_launch": bulk_ms},
         "step_roofline": {"achieved": step_bytes / (span_ms / steps * 1e-3) / 1e9,
                           "frac": step_bytes / (span_ms / steps * 1e-3) / 1e9 / peak,
