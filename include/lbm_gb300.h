@@ -211,6 +211,53 @@ lbm_status lbm_sync(lbm_solver *s);
  * stream capture. All calls share the array: calls that overlap on the GPU race. */
 lbm_status lbm_field_sums_static(const float *const fields[8], int64_t n, double *sums, void *stream);
 
+/* ---------------------------------------------------------------------------
+ * Gradients of time-averaged drag (no reference counterpart).
+ *
+ * A differentiable form of the LES step: the cylinder along z is the smoothed
+ * solid fraction phi = (1 + tanh((r - d)/width))/2 (d: distance to the axis
+ * (ox, oy)), used wherever the reference step uses its 0/1 solid test
+ * (bounce-back blend, momentum exchange, u = fluid j/rho, sponge sigma), all
+ * boundaries periodic, start state lbm_init (lbm.py:383-394). Runs on its own
+ * A/B population buffers in FP32 or FP64. The loss is
+ *   L = sum_{t = loss_start..steps} F_x(t) / (N_l 0.5 U^2 diameter nz),
+ * F_x(t) the momentum-exchange x force of step t, N_l the number of those
+ * steps. lbm_adj_backward runs the hand-written adjoint kernel backwards over
+ * the steps, recomputing each interval of `checkpoint` steps from the state
+ * the forward run kept at its start, and returns dL/d(U, tau0, Cs, r).
+ */
+typedef struct lbm_adj_config {
+    int32_t nx, ny, nz;
+    int32_t precision;           /* LBM_F32 | LBM_F64: storage and arithmetic */
+    int32_t steps;               /* steps of one forward run */
+    int32_t loss_start;          /* first step (1-based) whose force enters the loss */
+    int32_t checkpoint;          /* K: a state is kept every K steps */
+    int32_t device;
+    double u0, tau0, cs, r;      /* the parameters: inflow U, tau0 = 3 nu + 1/2, Cs, radius */
+    double ox, oy, width;        /* cylinder axis and tanh width */
+    double diameter;             /* length in the drag normalisation (a constant) */
+    double sponge_start, sponge_strength;
+    double seed_amp;             /* lbm_init's wave amplitude */
+} lbm_adj_config;
+
+typedef struct lbm_adj lbm_adj;
+
+/* Allocate the run: (steps/K + 1) checkpoints, K - 1 recompute states and the
+ * adjoint buffers, each 19 n values. */
+lbm_status lbm_adj_create(const lbm_adj_config *cfg, lbm_adj **out);
+lbm_status lbm_adj_destroy(lbm_adj *h);
+/* par = {U, tau0, Cs, r}; invalidates the last forward run. */
+lbm_status lbm_adj_set_params(lbm_adj *h, const double par[4]);
+/* Forward run from the start state; the loss (synchronous). */
+lbm_status lbm_adj_forward(lbm_adj *h, double *loss);
+/* dL/d(U, tau0, Cs, r) of the last forward run (synchronous). */
+lbm_status lbm_adj_backward(lbm_adj *h, double grad[4]);
+/* The state after `step` steps (a multiple of K, or 0) as 19 n values of the
+ * run's precision in the layout f[q*n + idx], to a host buffer. */
+lbm_status lbm_adj_state(lbm_adj *h, int32_t step, void *host);
+/* {forward ms, backward ms (CUDA events), sum of F_x over the loss steps, device bytes}. */
+lbm_status lbm_adj_info(lbm_adj *h, double out[4]);
+
 /* Message of the last error on this thread ("" when none). */
 const char *lbm_last_error(void);
 

@@ -51,6 +51,20 @@ class Config(ctypes.Structure):
     ]
 
 
+class AdjConfig(ctypes.Structure):
+    """struct lbm_adj_config."""
+
+    _fields_ = [
+        ("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32),
+        ("precision", ctypes.c_int32), ("steps", ctypes.c_int32), ("loss_start", ctypes.c_int32),
+        ("checkpoint", ctypes.c_int32), ("device", ctypes.c_int32),
+        ("u0", ctypes.c_double), ("tau0", ctypes.c_double), ("cs", ctypes.c_double), ("r", ctypes.c_double),
+        ("ox", ctypes.c_double), ("oy", ctypes.c_double), ("width", ctypes.c_double),
+        ("diameter", ctypes.c_double), ("sponge_start", ctypes.c_double),
+        ("sponge_strength", ctypes.c_double), ("seed_amp", ctypes.c_double),
+    ]
+
+
 _SIGNATURES = {
     "lbm_abi_version": (ctypes.c_int32, []),
     "lbm_last_error": (ctypes.c_char_p, []),
@@ -86,6 +100,13 @@ _SIGNATURES = {
                                              ctypes.c_void_p, ctypes.c_void_p]),
     "lbm_managed_alloc": (ctypes.c_int, [ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
     "lbm_managed_free": (ctypes.c_int, [ctypes.c_void_p]),
+    "lbm_adj_create": (ctypes.c_int, [ctypes.POINTER(AdjConfig), ctypes.POINTER(ctypes.c_void_p)]),
+    "lbm_adj_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "lbm_adj_set_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
+    "lbm_adj_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
+    "lbm_adj_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
+    "lbm_adj_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]),
+    "lbm_adj_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
 }
 
 _lib = None
