@@ -261,6 +261,28 @@ def run_reference(args):
 
 # ---------------------------------------------------------------------------
 
+def adjoint_timing(device):
+    """Gradient of the time-averaged drag coefficient of the LES cylinder at
+    Re 100, 256 x 128 x 32, 2000 steps (loss over steps 1001..2000),
+    checkpoints every 100 steps, FP32; r = 8 (tanh width 1.5), U = 0.05, Cs = 0.1.
+    Timed with CUDA events by the library after one untimed forward/backward."""
+    from adjoint import DragAdjoint
+    run = DragAdjoint(256, 128, 32, steps=2000, loss_start=1001, checkpoint=100, precision="f32",
+                      u0=0.05, reynolds=100.0, cs=0.1, r=8.0, width=1.5, device=device)
+    run.forward()
+    run.backward()
+    loss = run.forward()
+    grad = run.backward()
+    info = run.info()
+    cells = 256 * 128 * 32
+    return {"workload": "LES cylinder Re 100, 256x128x32, 2000 steps, K=100, FP32",
+            "loss": loss, "grad": {k: float(v) for k, v in zip(("U", "tau0", "Cs", "r"), grad)},
+            "forward_ms": info["forward_ms"], "backward_ms": info["backward_ms"],
+            "backward_over_forward": info["backward_ms"] / info["forward_ms"],
+            "forward_glups": cells * 2000 / (info["forward_ms"] * 1e-3) / 1e9,
+            "device_bytes": info["device_bytes"]}
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -274,6 +296,8 @@ def main():
     ap.add_argument("--report", action="store_true",
                     help="time report steps (13 diagnostic fields and FP64 monitor sums every step)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true",
+                    help="skip the drag-adjoint timing (256x128x32, 2000 steps, FP32)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -357,6 +381,9 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         f = s.populations(np.float32)
         line["cpu_baseline"] = cpu_baseline_single(f)
+    if not args.no_adjoint:
+        del s
+        line["adjoint"] = adjoint_timing(local)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:

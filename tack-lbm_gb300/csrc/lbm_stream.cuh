@@ -1,4 +1,4 @@
-// lbm_stream.cuh - the bulk-copy (TMA) fed AA step: the main sm_103a kernel.
+// lbm_stream.cuh - the bulk-copy (TMA) fed AA step kernel (LBM_FLAG_BULKCOPY).
 //
 // The lattice is cut into row segments: SW consecutive cells of one x-row
 // (y, z). A persistent CTA of SW threads walks its share of segments. For each
