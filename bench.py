@@ -296,6 +296,9 @@ def main():
     ap.add_argument("--report", action="store_true",
                     help="time report steps (13 diagnostic fields and FP64 monitor sums every step)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--study", choices=["c2", "c3", "c5"],
+                    help="run a physics/precision study instead of the benchmark (one JSON line)")
+    ap.add_argument("--study-steps", type=int, default=None)
     ap.add_argument("--no-adjoint", action="store_true",
                     help="skip the drag-adjoint timing (256x128x32, 2000 steps, FP32)")
     args = ap.parse_args()
@@ -303,6 +306,11 @@ def main():
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
         return run_reference(args)
+    if args.study:
+        import studies
+        kw = {} if args.study_steps is None else {"steps": args.study_steps}
+        print(json.dumps(studies.STUDIES[args.study](**kw)), flush=True)
+        return 0
 
     world, rank, local, dist, torch = dist_setup(args.gpus)
     import lbm_native as N
