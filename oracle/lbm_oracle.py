@@ -53,6 +53,15 @@ MIRZ = _table(np.array([1, 1, -1]))
 
 FIELDS = ("ux", "uy", "uz", "p", "vmag", "r_rho", "r_ux", "r_uy", "r_uz", "r_ke", "fx", "fy", "fz")
 
+# D3Q7 for temperature (lbm.py:20-25): rest plus the six faces, float32 weights
+CX7 = np.array([0, 1, -1, 0, 0, 0, 0])
+CY7 = np.array([0, 0, 0, 1, -1, 0, 0])
+CZ7 = np.array([0, 0, 0, 0, 0, 1, -1])
+W7 = np.array([1 / 4] + [1 / 8] * 6, np.float32).astype(np.float64)
+OPP7 = np.array([0, 2, 1, 4, 3, 6, 5])
+PR_T = 0.85  # turbulent Prandtl number (lbm.py:285)
+HEAT_FIELDS = ("t_solid", "q_solid", "temp")
+
 
 @dataclass
 class Config:
@@ -80,6 +89,13 @@ class Config:
     lateral: str = "periodic"       # "periodic" | "slip" | "lid"
     vertical: str = "periodic"      # "periodic" | "slip"
     u_lid: float = 0.0
+    # HeatSink (lbm.py:230-276): x0, length, z0, width, base, fin_height,
+    # fin_thickness, fin_pitch, in cells
+    sink: tuple = (0, 0, 0, 0, 0, 0, 1, 1)
+    # D3Q7 temperature (lbm.py:279-319, lbm.py:457-492)
+    heat: bool = False
+    alpha: float = 0.0              # molecular diffusivity (nu / prandtl at construction)
+    heat_nu: float = 0.0            # the viscosity the subgrid diffusivity subtracts
 
     @property
     def n(self):
@@ -124,7 +140,25 @@ def solid(cfg, x, y, z, precision="f64"):
         d = np.maximum(np.maximum(np.abs(x - t(cfg.ox)) - t(cfg.hx), np.abs(y - t(cfg.oy)) - t(cfg.hy)),
                        np.abs(z - t(cfg.oz)) - t(cfg.hz))
         return (d < 0).astype(np.float64)
+    if cfg.obstacle == "heatsink":
+        wall = ((y <= 0) | (y >= cfg.ny - 1)).astype(np.float64)
+        return np.maximum(wall, sink(cfg, x, y, z))
     return np.zeros(np.broadcast(x, y, z).shape)
+
+
+def sink(cfg, x, y, z):
+    """HeatSink.sink (lbm.py:250-261): base plate and fins of the sink, 1.0 or 0.0.
+    Integer coordinates; zero for every other obstacle."""
+    if cfg.obstacle != "heatsink":
+        return np.zeros(np.broadcast(x, y, z).shape)
+    x0, length, z0, width, base, fin_h, fin_t, pitch = cfg.sink
+    x1, z1 = x0 + length, z0 + width
+    y_base, y_top = 1.0 + base, 1.0 + base + fin_h
+    fx, fy, fz = (np.asarray(a, np.float64) for a in (x, y, z))
+    inside = (fx >= x0) & (fx < x1) & (fz >= z0) & (fz < z1) & (fy >= 1.0)
+    base_p = fy < y_base
+    fin = (fy < y_top) & (np.mod(np.asarray(z, np.int64) - int(z0), int(pitch)) < fin_t)
+    return (inside & (base_p | fin)).astype(np.float64)
 
 
 def wall_velocity(cfg, xm, ym, zm):
@@ -250,6 +284,67 @@ def step(cfg, f_in, fields=None, report=False, cells=None, dtype=np.float64):
     ``report=True`` the 13 diagnostic fields in ``fields`` (a dict of length-n
     arrays, the previous report's values) are updated for those cells.
     """
+    return _step(cfg, f_in, fields, report, cells, dtype)[0]
+
+
+def step_heat(cfg, f_in, g_in, t_solid, fields=None, heat_fields=None, report=False, dtype=np.float64):
+    """One ``lbm_step`` with the D3Q7 temperature block (lbm.py:457-492).
+
+    ``g_in`` holds 7*n temperature populations ``g[q*n + idx]``, ``t_solid``
+    the solid temperature per cell. Returns (f_out, g_out) as (19, n) and
+    (7, n) arrays. With ``report=True`` ``heat_fields["temp"]`` is written and
+    ``heat_fields["q_solid"]`` receives each fluid cell's temperature on the
+    sink voxels it faces (lbm.py:484-492; the caller zeroes it first, as
+    Solver.step does, lbm.py:641-642).
+    """
+    n = cfg.n
+    out, e = _step(cfg, f_in, fields, report, None, dtype)
+    G = np.asarray(g_in).reshape(7, n).astype(dtype, copy=False)
+    ts = np.asarray(t_solid, dtype)
+    x, y, z, idx = e["x"], e["y"], e["z"], e["idx"]
+    nx, ny, nz = cfg.nx, cfg.ny, cfg.nz
+    g = np.empty((7, n), dtype)
+    temp = np.zeros(n, dtype)
+    for q in range(7):
+        o = OPP7[q]
+        xs = (x - CX7[q] + nx) % nx
+        ys = (y - CY7[q] + ny) % ny
+        zs = (z - CZ7[q] + nz) % nz
+        nidx = (zs * ny + ys) * nx + xs
+        wall = solid(cfg, xs, ys, zs).astype(dtype)
+        hot = sink(cfg, xs, ys, zs).astype(dtype)
+        pulled = G[q, nidx]
+        bounced = G[o, idx]
+        at_wall = bounced * (1.0 - 2.0 * hot) + hot * 2.0 * W7[q] * ts[nidx]
+        g[q] = pulled + wall * (at_wall - pulled)
+        temp = temp + g[q]
+    tau = e["tau"]
+    alpha = cfg.alpha + np.maximum(0.0, (tau - 0.5) / 3.0 - cfg.heat_nu) / PR_T
+    omega_g = 1.0 / (4.0 * alpha + 0.5)
+    sigma = e["sigma"]
+    temp_s = (1.0 - sigma) * temp
+    ux, uy, uz = e["ux"], e["uy"], e["uz"]
+    usx, usy, usz = e["ux_s"], e["uy_s"], e["uz_s"]
+    g_out = np.empty_like(g)
+    for q in range(7):
+        eq = W7[q] * temp * (1.0 + 4.0 * (CX7[q] * ux + CY7[q] * uy + CZ7[q] * uz))
+        post = g[q] - omega_g * (g[q] - eq)
+        es = W7[q] * temp_s * (1.0 + 4.0 * (CX7[q] * usx + CY7[q] * usy + CZ7[q] * usz))
+        g_out[q] = es + (1.0 - sigma) * (post - eq)
+    if report:
+        fluid, here = e["fluid"], e["here"]
+        heat_fields["temp"][idx] = fluid * temp + here * ts[idx]
+        for q in range(1, 7):
+            xs = (x - CX7[q] + nx) % nx
+            ys = (y - CY7[q] + ny) % ny
+            zs = (z - CZ7[q] + nz) % nz
+            nidx = (zs * ny + ys) * nx + xs
+            hot = sink(cfg, xs, ys, zs)
+            np.add.at(heat_fields["q_solid"], nidx, fluid * hot * temp)
+    return out, g_out
+
+
+def _step(cfg, f_in, fields, report, cells, dtype):
     n = cfg.n
     F = np.asarray(f_in).reshape(19, n).astype(dtype, copy=False)
     idx = np.arange(n) if cells is None else np.asarray(cells)
@@ -295,7 +390,7 @@ def step(cfg, f_in, fields=None, report=False, cells=None, dtype=np.float64):
     ux = fluid * jx / rho
     uy = fluid * jy / rho
     uz = fluid * jz / rho
-    post, _tau = collide(cfg, f, rho, ux, uy, uz)
+    post, tau = collide(cfg, f, rho, ux, uy, uz)
     s0 = dtype(cfg.sponge_start)
     t = np.maximum(dtype(0.0), (x.astype(dtype) - s0) / (dtype(nx) - s0))
     sigma = np.maximum(here, dtype(cfg.sponge_strength) * t * t)
@@ -326,7 +421,9 @@ def step(cfg, f_in, fields=None, report=False, cells=None, dtype=np.float64):
         d["fx"][idx] = mx
         d["fy"][idx] = my
         d["fz"][idx] = mz
-    return out
+    extras = dict(x=x, y=y, z=z, idx=idx, here=here, fluid=fluid, tau=tau, ux=ux, uy=uy, uz=uz,
+                  sigma=sigma, ux_s=ux_s, uy_s=uy_s, uz_s=uz_s)
+    return out, extras
 
 
 def new_fields(n, dtype=np.float64):

@@ -17,6 +17,8 @@ stores as float32 are given float32 values on input). The script writes:
 * ``solver_cases.npz`` - whole ``Solver`` runs: construction (init plus the
                       priming report step), quiet and report steps, a rotation
                       change and ``monitors()``.
+* ``heat_cases.npz``- one ``lbm_step`` with the D3Q7 temperature block (``Heat``)
+                      over the finned ``HeatSink``, quiet and report.
 
 Nothing reads the reference at test time; only these files are used.
 """
@@ -164,6 +166,90 @@ def make_init_cases(ref_dir):
     np.savez_compressed(os.path.join(HERE, "init_cases.npz"), **out)
 
 
+# (name, collision, report): one step with the D3Q7 temperature block over the
+# finned heat sink, at the reference Solver's HeatSink placement (lbm.py:635-637)
+HEAT_CASES = [("heat_les_report", "les", True), ("heat_trt_quiet", "trt", False),
+              ("heat_bgk_report", "bgk", True)]
+HNX, HNY, HNZ, HD = 20, 12, 16, 6.0
+
+
+def heatsink_params(nx, ny, nz, d):
+    """The HeatSink arguments Solver.set_obstacle("heatsink") passes (lbm.py:635-637)."""
+    return (int(0.2 * nx), int(0.3 * nx), int(0.125 * nz), int(0.75 * nz), round(d / 2), int(0.45 * ny),
+            round(d / 3), round(d))
+
+
+def make_heat_cases(ref_dir):
+    lbm = tack_shim.import_reference(ref_dir)
+    n = HNX * HNY * HNZ
+    sink = heatsink_params(HNX, HNY, HNZ, HD)
+    out, meta = {}, {}
+    for k, (name, coll, report) in enumerate(HEAT_CASES):
+        rng = np.random.default_rng(300 + k)
+        lat = lbm.D3Q19(HNX, HNY, HNZ)
+        nu = 0.01 + 0.003 * k
+        phys = lbm.COLLISIONS[coll](nu)
+        geo = lbm.HeatSink(HNY, *sink)
+        omega = tack_shim.HostManagedArray(1)
+        u0, s0, strength = 0.05, 15.0, 0.8
+        flow = lbm.Flow(u0, s0, strength, omega.tack, lbm.PeriodicY())
+        idx = np.arange(n)
+        x, y, z = idx % HNX, (idx // HNX) % HNY, idx // (HNX * HNY)
+        solid = np.array([geo.solid(int(a), int(b), int(c)) for a, b, c in zip(x, y, z)])
+        hot = np.array([geo.sink(int(a), int(b), int(c)) for a, b, c in zip(x, y, z)])
+        cvec = np.array([lbm.CX, lbm.CY, lbm.CZ]).T
+        w = np.array(lbm.W, np.float32).astype(np.float64)
+        rho = 1 + 0.01 * rng.standard_normal(n)
+        u = np.array([u0, 0.0, 0.0]) + 0.02 * rng.standard_normal((n, 3))
+        cu = 3.0 * (u @ cvec.T)
+        f = w * rho[:, None] * (1 + cu + 0.5 * cu ** 2 - 1.5 * (u ** 2).sum(1)[:, None])
+        f += 1e-3 * rng.standard_normal((n, 19))
+        f[solid > 0] = w
+        f_in = np.ascontiguousarray(f.T.reshape(-1)).astype(np.float32)
+        # temperature populations near w7 T with T in [0, 1]; zero in solid cells
+        w7 = np.array(lbm.W7, np.float32).astype(np.float64)
+        temp = rng.uniform(0.0, 1.0, n)
+        g = w7 * temp[:, None] + 0.01 * rng.standard_normal((n, 7))
+        g[solid > 0] = 0.0
+        g_in = np.ascontiguousarray(g.T.reshape(-1)).astype(np.float32)
+        t_solid = np.where(hot > 0, rng.uniform(0.5, 1.5, n), 0.0).astype(np.float32)
+        fields = {key: tack_shim.HostManagedArray(n) for key in lbm.FIELDS}
+        prev = {key: fields[key].numpy.copy() for key in lbm.FIELDS}
+        diag = (lbm.Report if report else lbm.Quiet)({k_: v.tack for k_, v in fields.items()})
+        st = lbm.Solver.__new__(lbm.Solver)
+        st.heat_enabled, st.nu, st.prandtl, st.nx = True, nu, 0.7, HNX
+        st._setup_heat(n)
+        st.heat_fields["t_solid"].numpy[:] = t_solid
+        st.heat_fields["q_solid"].numpy[:] = 0.0
+        a_in = lbm.tack.array(f_in)
+        a_out = lbm.tack.empty((19 * n,))
+        g_a = lbm.tack.array(g_in)
+        g_b = lbm.tack.zeros((7 * n,))
+        t0 = time.perf_counter()
+        lbm.lbm_step(lat, phys, geo, flow, diag, a_in, a_out, st.heat, g_a, g_b)
+        print(f"{name}: {time.perf_counter() - t0:.2f} s, solid {int(solid.sum())}, sink {int(hot.sum())}")
+        out[f"{name}/f_in"] = f_in
+        out[f"{name}/g_in"] = g_in
+        out[f"{name}/t_solid"] = t_solid
+        out[f"{name}/f_out"] = np.asarray(a_out)
+        out[f"{name}/g_out"] = np.asarray(g_b)
+        out[f"{name}/solid"] = solid.astype(np.uint8)
+        out[f"{name}/sink"] = hot.astype(np.uint8)
+        if report:
+            out[f"{name}/temp"] = np.asarray(st.heat_fields["temp"].numpy)
+            out[f"{name}/q_solid"] = np.asarray(st.heat_fields["q_solid"].numpy)
+            for key in lbm.FIELDS:
+                out[f"{name}/fields/{key}"] = np.asarray(fields[key].numpy)
+        for key in lbm.FIELDS:
+            out[f"{name}/prev/{key}"] = prev[key].astype(np.float32)
+        meta[name] = dict(nx=HNX, ny=HNY, nz=HNZ, collision=coll, nu=nu, obstacle="heatsink",
+                          lateral="periodic", report=report, u0=u0, sponge_start=s0,
+                          sponge_strength=strength, sink=list(sink), heat=True, alpha=nu / 0.7,
+                          heat_nu=nu)
+    out["meta"] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(HERE, "heat_cases.npz"), **out)
+
+
 def make_solver_cases(ref_dir):
     lbm = tack_shim.import_reference(ref_dir)
     out, meta = {}, {}
@@ -200,6 +286,7 @@ def main():
     make_step_cases(ref_dir)
     make_init_cases(ref_dir)
     make_solver_cases(ref_dir)
+    make_heat_cases(ref_dir)
 
 
 if __name__ == "__main__":

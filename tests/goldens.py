@@ -39,3 +39,23 @@ def step_cases():
         if m["report"]:
             case["fields"] = {k: z[f"{name}/fields/{k}"] for k in O.FIELDS}
         yield case
+
+
+def heat_case_config(m):
+    keys = ("collision", "nu", "obstacle", "lateral", "u0", "sponge_start", "sponge_strength",
+            "alpha", "heat_nu")
+    return O.Config(m["nx"], m["ny"], m["nz"], sink=tuple(m["sink"]), heat=True,
+                    **{k: m[k] for k in keys})
+
+
+def heat_cases():
+    z, meta = load("heat_cases")
+    for name, m in meta.items():
+        case = {"name": name, "cfg": heat_case_config(m), "report": m["report"],
+                **{k: z[f"{name}/{k}"] for k in ("f_in", "g_in", "t_solid", "f_out", "g_out", "solid", "sink")},
+                "prev": {k: z[f"{name}/prev/{k}"] for k in O.FIELDS}}
+        if m["report"]:
+            case["temp"] = z[f"{name}/temp"]
+            case["q_solid"] = z[f"{name}/q_solid"]
+            case["fields"] = {k: z[f"{name}/fields/{k}"] for k in O.FIELDS}
+        yield case

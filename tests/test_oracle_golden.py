@@ -119,3 +119,25 @@ def test_float32_mode_close_to_float64():
         fields = {k: v.astype(np.float32) for k, v in case["prev"].items()}
         out = O.step(case["cfg"], case["f_in"], fields, report=case["report"], dtype=np.float32)
         assert weight_err(out, case["f_out"]) < 1e-6, case["name"]
+
+
+@pytest.mark.parametrize("case", list(goldens.heat_cases()), ids=lambda c: c["name"])
+def test_heat_step_golden(case):
+    """The D3Q7 temperature block over the heat sink (lbm.py:457-492) against
+    the reference kernel's own output: masks exact, populations, temperature
+    and the wall heat sums to float64 round-off."""
+    cfg = case["cfg"]
+    assert np.array_equal(O.mask(cfg).astype(np.uint8), case["solid"])
+    idx = np.arange(cfg.n)
+    sink = O.sink(cfg, idx % cfg.nx, (idx // cfg.nx) % cfg.ny, idx // (cfg.nx * cfg.ny))
+    assert np.array_equal(sink.astype(np.uint8), case["sink"])
+    fields = {k: v.astype(np.float64) for k, v in case["prev"].items()}
+    heat = {k: np.zeros(cfg.n) for k in O.HEAT_FIELDS}
+    f, g = O.step_heat(cfg, case["f_in"], case["g_in"], case["t_solid"], fields, heat, report=case["report"])
+    assert np.abs(f.reshape(-1) - case["f_out"]).max() < 1e-12
+    assert np.abs(g.reshape(-1) - case["g_out"]).max() < 1e-12
+    if case["report"]:
+        assert np.abs(heat["temp"] - case["temp"]).max() < 1e-12
+        assert np.abs(heat["q_solid"] - case["q_solid"]).max() < 1e-11
+        for k in O.FIELDS:
+            assert np.abs(fields[k] - case["fields"][k]).max() < 1e-12, k
