@@ -42,8 +42,15 @@ typedef enum lbm_status {
 
 /* collision models: the COLLISIONS registry (lbm.py:544) */
 enum { LBM_BGK = 0, LBM_TRT = 1, LBM_LES = 2 };
-/* obstacles (lbm.py:144-227); LBM_NO_OBSTACLE has no solid cell */
-enum { LBM_NO_OBSTACLE = 0, LBM_CYLINDER = 1, LBM_SPHERE = 2, LBM_BOX = 3 };
+/* obstacles (lbm.py:144-276); LBM_NO_OBSTACLE has no solid cell; LBM_HEATSINK is the
+ * finned sink on the floor of a duct with walls at y = 0 and y = ny - 1 (HeatSink) */
+enum { LBM_NO_OBSTACLE = 0, LBM_CYLINDER = 1, LBM_SPHERE = 2, LBM_BOX = 3, LBM_HEATSINK = 4 };
+/* temperature fields of a heat run (Solver.heat_fields, lbm.py:586-604): the solid's
+ * temperature (input), the summed fluid temperature on each wetted sink voxel, the
+ * temperature (report steps) */
+enum { LBM_T_SOLID = 0, LBM_Q_SOLID = 1, LBM_TEMP = 2, LBM_NUM_HEAT_FIELDS = 3 };
+/* output grid fields: ux, uy, uz, p, vmag, and temp when the run has heat */
+enum { LBM_OUT_TEMP = 5, LBM_MAX_OUTPUTS = 6 };
 /* y boundaries: PeriodicY / SlipY (lbm.py:342-369); LID adds a moving no-slip top wall (new) */
 enum { LBM_PERIODIC = 0, LBM_SLIP = 1, LBM_LID = 2 };
 /* population storage on the device: FP32, FP16/BF16 deviations f - w_q, FP64 (oracle runs) */
@@ -81,6 +88,17 @@ typedef struct lbm_config {
     double omega_rot;            /* cylinder surface speed (lbm.py:618-620) */
     int32_t device;              /* CUDA device ordinal */
     int32_t flags;               /* LBM_FLAG_* */
+    /* LBM_HEATSINK geometry in cells, the HeatSink arguments (lbm.py:235-244)
+     * Solver.set_obstacle passes (lbm.py:635-637): x0, length, z0, width, base,
+     * fin_height, fin_thickness, fin_pitch */
+    double sink[8];
+    /* heat != 0 adds the D3Q7 temperature (lbm.py:457-492; FP32 storage and the
+     * per-cell kernels only): alpha is the molecular diffusivity, heat_nu the
+     * viscosity its subgrid part subtracts (Heat(arrays, nu/prandtl, nu), lbm.py:596-599) */
+    int32_t heat;
+    int32_t reserved;
+    double alpha;
+    double heat_nu;
 } lbm_config;
 
 /* lbm_config.flags: LBM_FLAG_BULKCOPY selects the bulk-copy (TMA) staged step
@@ -134,9 +152,14 @@ lbm_status lbm_field(lbm_solver *s, int32_t id, float **ptr);
 /* Change collision model and viscosity; cs < 0 keeps the current constant (lbm.py:613-616). */
 lbm_status lbm_set_physics(lbm_solver *s, int32_t collision, double nu, double cs);
 
-/* Change the obstacle: geo = {ox, oy, oz, r, hx, hy, hz}. The populations are
- * carried over as the reference does (lbm.py:628-637). */
+/* Change the obstacle: geo = {ox, oy, oz, r, hx, hy, hz} (LBM_HEATSINK takes its
+ * geometry from lbm_config.sink). The populations are carried over as the
+ * reference does (lbm.py:628-637). */
 lbm_status lbm_set_obstacle(lbm_solver *s, int32_t kind, const double geo[7]);
+
+/* Set the heat-sink geometry (lbm_config.sink order); when the obstacle is
+ * LBM_HEATSINK the new sink takes effect as lbm_set_obstacle would. */
+lbm_status lbm_set_sink(lbm_solver *s, const double sink[8]);
 
 /* Cylinder surface speed, stream-ordered with the steps (lbm.py:618-624). */
 lbm_status lbm_set_actuation(lbm_solver *s, double omega_rot);
@@ -156,7 +179,8 @@ lbm_status lbm_get_populations(lbm_solver *s, void *f, int32_t dtype, int32_t wh
  * axis, (d + stride - 1)/stride points per axis, in managed memory
  * (lbm.py:574-581). stride 1 aliases the full-resolution fields. */
 lbm_status lbm_set_output_stride(lbm_solver *s, int32_t stride);
-/* Managed pointer to output field `id` (LBM_UX .. LBM_VMAG) and its point count. */
+/* Managed pointer to output field `id` (LBM_UX .. LBM_VMAG, LBM_OUT_TEMP with heat)
+ * and its point count. */
 lbm_status lbm_output(lbm_solver *s, int32_t id, float **ptr, int64_t *count);
 /* Refresh the output fields from the full-resolution ones: the coarsen kernel
  * (lbm.py:516-522) for every output field (Solver.update_output, lbm.py:606-611). */
@@ -257,6 +281,16 @@ lbm_status lbm_adj_backward(lbm_adj *h, double grad[4]);
 lbm_status lbm_adj_state(lbm_adj *h, int32_t step, void *host);
 /* {forward ms, backward ms (CUDA events), sum of F_x over the loss steps, device bytes}. */
 lbm_status lbm_adj_info(lbm_adj *h, double out[4]);
+
+/* Managed pointer to heat field `id` (LBM_T_SOLID, LBM_Q_SOLID, LBM_TEMP; n floats),
+ * valid until lbm_destroy. LBM_ERR_STATE when the run has no heat. Report steps zero
+ * q_solid before they add to it (Solver.step, lbm.py:641-642). */
+lbm_status lbm_heat_field(lbm_solver *s, int32_t id, float **ptr);
+
+/* Copy the temperature populations in/out in the layout g[q*n + idx] (7*n values,
+ * D3Q7 order of lbm.py:20-25). They start at zero (lbm.py:592). */
+lbm_status lbm_set_heat_populations(lbm_solver *s, const void *g, int32_t dtype, int32_t where);
+lbm_status lbm_get_heat_populations(lbm_solver *s, void *g, int32_t dtype, int32_t where);
 
 /* Message of the last error on this thread ("" when none). */
 const char *lbm_last_error(void);

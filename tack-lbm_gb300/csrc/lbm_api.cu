@@ -62,8 +62,16 @@ lbm_status validate(const lbm_config &g) {
     return fail(LBM_ERR_ARG, "ny/4 and nz must be <= 65535");
   if (g.collision < LBM_BGK || g.collision > LBM_LES)
     return fail(LBM_ERR_ARG, "unknown collision model (bgk=0, trt=1, les=2)");
-  if (g.obstacle < LBM_NO_OBSTACLE || g.obstacle > LBM_BOX)
-    return fail(LBM_ERR_ARG, "unknown obstacle (none=0, cylinder=1, sphere=2, box=3)");
+  if (g.obstacle < LBM_NO_OBSTACLE || g.obstacle > LBM_HEATSINK)
+    return fail(LBM_ERR_ARG, "unknown obstacle (none=0, cylinder=1, sphere=2, box=3, heatsink=4)");
+  for (double v : g.sink)
+    if (!std::isfinite(v) || v < 0.0 || v > 1e9) return fail(LBM_ERR_ARG, "heat sink sizes must be finite and >= 0");
+  if (g.obstacle == LBM_HEATSINK && !(g.sink[7] >= 1.0)) return fail(LBM_ERR_ARG, "heat sink fin pitch must be >= 1");
+  if (g.heat) {
+    if (g.storage != LBM_F32) return fail(LBM_ERR_ARG, "heat needs FP32 population storage");
+    if (!(std::isfinite(g.alpha) && g.alpha >= 0.0 && std::isfinite(g.heat_nu)))
+      return fail(LBM_ERR_ARG, "heat diffusivity must be finite and >= 0");
+  }
   if (g.lateral < LBM_PERIODIC || g.lateral > LBM_LID)
     return fail(LBM_ERR_ARG, "unknown lateral policy (periodic=0, slip=1, lid=2)");
   if (g.vertical != LBM_PERIODIC && g.vertical != LBM_SLIP)
@@ -95,6 +103,11 @@ void obstacle_box(const lbm_config &g, Range r[3], bool &any) {
     h[1] = g.hy;
     h[2] = g.hz;
     if (!(g.hx > 0 && g.hy > 0 && g.hz > 0)) any = false;
+  } else if (g.obstacle == LBM_HEATSINK) {
+    // duct walls at y = 0 and ny - 1 along the whole lattice
+    const int64_t dims[3] = {g.nx, g.ny, g.nz};
+    for (int k = 0; k < 3; ++k) r[k] = {0, dims[k] - 1};
+    return;
   } else {
     any = false;
   }
@@ -261,8 +274,8 @@ void place_on_device(void *p, size_t bytes, int device) {
 
 void release_output(Ctx &c) {
   if (c.out_stride > 1)
-    for (int k = 0; k < 5; ++k) cudaFree(c.out[k]);
-  for (int k = 0; k < 5; ++k) c.out[k] = c.fld[k];
+    for (int k = 0; k < c.nout; ++k) cudaFree(c.out[k]);
+  for (int k = 0; k < LBM_MAX_OUTPUTS; ++k) c.out[k] = k < c.nout ? lbmh::output_source(c, k) : nullptr;
   c.out_stride = 1;
   c.out_dims[0] = c.cfg.nx;
   c.out_dims[1] = c.cfg.ny;
@@ -295,6 +308,10 @@ void release(lbm_solver *s) {
   if (c.join) cudaEventDestroy(c.join);
   cudaFree(c.F);
   for (int k = 0; k < LBM_NUM_FIELDS; ++k) cudaFree(c.fld[k]);
+  cudaFree(c.g[0]);
+  cudaFree(c.g[1]);
+  cudaFree(c.aux);
+  for (int k = 0; k < LBM_NUM_HEAT_FIELDS; ++k) cudaFree(c.heat_fld[k]);
   cudaFree(c.partials);
   cudaFree(c.stage);
   cudaFree(c.sums);
@@ -352,10 +369,11 @@ __global__ void mask_kernel(lbmk::Geo geo, int nx, int ny, int n, uint8_t *out) 
   }
 }
 
-// coarsen (lbm.py:516-522): dst[(k*my + j)*mx + i] = src[((k*s)*ny + j*s)*nx + i*s] for 5 fields
+// coarsen (lbm.py:516-522): dst[(k*my + j)*mx + i] = src[((k*s)*ny + j*s)*nx + i*s] per output field
 struct CoarsenArgs {
-  const float *src[5];
-  float *dst[5];
+  const float *src[LBM_MAX_OUTPUTS];
+  float *dst[LBM_MAX_OUTPUTS];
+  int count;
 };
 
 __global__ void coarsen_kernel(CoarsenArgs a, int nx, int ny, int s, int mx, int my, int m) {
@@ -363,15 +381,17 @@ __global__ void coarsen_kernel(CoarsenArgs a, int nx, int ny, int s, int mx, int
     const int i = idx % mx, j = (idx / mx) % my, k = idx / (mx * my);
     const int src = ((k * s) * ny + j * s) * nx + i * s;
 #pragma unroll
-    for (int f = 0; f < 5; ++f) a.dst[f][idx] = a.src[f][src];
+    for (int f = 0; f < LBM_MAX_OUTPUTS; ++f)
+      if (f < a.count) a.dst[f][idx] = a.src[f][src];
   }
 }
 
 cudaError_t launch_coarsen(const Ctx &c, cudaStream_t st) {
   if (c.out_stride <= 1) return cudaSuccess;
-  CoarsenArgs a;
-  for (int f = 0; f < 5; ++f) {
-    a.src[f] = c.fld[f];
+  CoarsenArgs a{};
+  a.count = c.nout;
+  for (int f = 0; f < c.nout; ++f) {
+    a.src[f] = output_source(c, f);
     a.dst[f] = c.out[f];
   }
   const int m = c.out_dims[0] * c.out_dims[1] * c.out_dims[2];
@@ -392,7 +412,7 @@ cudaError_t launch_mask(const Ctx &c, uint8_t *dst, cudaStream_t st) {
 
 extern "C" {
 
-int32_t lbm_abi_version(void) { return 1; }
+int32_t lbm_abi_version(void) { return 2; }
 
 const char *lbm_last_error(void) { return g_err.c_str(); }
 
@@ -416,7 +436,7 @@ lbm_status lbm_create(const lbm_config *cfg, lbm_solver **out) {
     // the bulk-copy kernel moves 16-byte pieces: rows must split into them
     const int h = 16 / (int)storage_bytes(cfg->storage);
     const int tail = cfg->nx % lbmk::SW;
-    c.use_stream = (cfg->flags & LBM_FLAG_BULKCOPY) && !(cfg->flags & LBM_FLAG_SIMT) && cfg->nx % h == 0 &&
+    c.use_stream = (cfg->flags & LBM_FLAG_BULKCOPY) && !(cfg->flags & LBM_FLAG_SIMT) && !cfg->heat && cfg->nx % h == 0 &&
                    cfg->nx >= 2 * h && (tail == 0 || tail >= 2 * h);
     c.nseg_x = (cfg->nx + lbmk::SW - 1) / lbmk::SW;
     c.nseg = c.nseg_x * cfg->ny * cfg->nz;
@@ -454,6 +474,23 @@ lbm_status lbm_create(const lbm_config *cfg, lbm_solver **out) {
     if (e == cudaSuccess) e = cudaMemset(c.fld[k], 0, (size_t)c.n * sizeof(float));
     if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("cudaMallocManaged: ") + cudaGetErrorString(e)));
     s->bytes += c.n * (int64_t)sizeof(float);
+  }
+  c.nout = cfg->heat ? 6 : 5;
+  if (cfg->heat) {
+    const size_t gbytes = (size_t)7 * (size_t)c.n * sizeof(float);
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+      e = cudaMalloc(&c.g[k], gbytes);
+      if (e == cudaSuccess) e = cudaMemset(c.g[k], 0, gbytes);
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&c.aux, (size_t)c.n * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMemset(c.aux, 0, (size_t)c.n * sizeof(float4));
+    for (int k = 0; k < LBM_NUM_HEAT_FIELDS && e == cudaSuccess; ++k) {
+      e = cudaMallocManaged(&c.heat_fld[k], (size_t)c.n * sizeof(float), cudaMemAttachGlobal);
+      if (e == cudaSuccess) place_on_device(c.heat_fld[k], (size_t)c.n * sizeof(float), cfg->device);
+      if (e == cudaSuccess) e = cudaMemset(c.heat_fld[k], 0, (size_t)c.n * sizeof(float));
+    }
+    if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("heat buffers: ") + cudaGetErrorString(e)));
+    s->bytes += 2 * (int64_t)gbytes + c.n * (int64_t)(sizeof(float4) + LBM_NUM_HEAT_FIELDS * sizeof(float));
   }
   // fast-kernel blocks plus at most one general block per four warps
   c.partial_rows = std::max<int64_t>(2 * c.nblocks + 1, (int64_t)c.num_sms * 32);
@@ -518,6 +555,10 @@ lbm_status lbm_init_random(lbm_solver *s, double rho_sigma, double u_noise, uint
 lbm_status lbm_step(lbm_solver *s, int32_t report, void *stream) {
   LBM_HANDLE(s);
   LBM_CUDA(dispatch_step(s->c, report != 0, (cudaStream_t)stream));
+  if (s->c.cfg.heat) {
+    LBM_CUDA(lbmh::launch_heat(s->c, report != 0, (cudaStream_t)stream));
+    s->c.g_cur ^= 1;
+  }
   if (s->c.ev && s->c.ev_used < s->c.ev_cap) s->c.ev_used++;
   s->c.odd_next ^= 1;
   s->steps += 1;
@@ -531,6 +572,10 @@ lbm_status lbm_run(lbm_solver *s, int32_t count, int32_t report_last, void *stre
   for (int32_t k = 0; k < count; ++k) {
     const bool rep = report_last && k == count - 1;
     LBM_CUDA(dispatch_step(s->c, rep, (cudaStream_t)stream));
+    if (s->c.cfg.heat) {
+      LBM_CUDA(lbmh::launch_heat(s->c, rep, (cudaStream_t)stream));
+      s->c.g_cur ^= 1;
+    }
     if (s->c.ev && s->c.ev_used < s->c.ev_cap) s->c.ev_used++;
     s->c.odd_next ^= 1;
     s->steps += 1;
@@ -727,13 +772,13 @@ lbm_status lbm_set_output_stride(lbm_solver *s, int32_t stride) {
     c.out_dims[k] = (dims[k] + stride - 1) / stride;
     m *= (size_t)c.out_dims[k];
   }
-  for (int k = 0; k < 5; ++k) {
+  for (int k = 0; k < c.nout; ++k) {
     c.out[k] = nullptr;
     cudaError_t e = cudaMallocManaged(&c.out[k], m * sizeof(float), cudaMemAttachGlobal);
     if (e == cudaSuccess) place_on_device(c.out[k], m * sizeof(float), c.cfg.device);
     if (e != cudaSuccess) {
       for (int j = 0; j < k; ++j) cudaFree(c.out[j]);
-      for (int j = 0; j < 5; ++j) c.out[j] = c.fld[j];
+      for (int j = 0; j < c.nout; ++j) c.out[j] = lbmh::output_source(c, j);
       c.out_dims[0] = c.cfg.nx;
       c.out_dims[1] = c.cfg.ny;
       c.out_dims[2] = c.cfg.nz;
@@ -748,7 +793,8 @@ lbm_status lbm_set_output_stride(lbm_solver *s, int32_t stride) {
 
 lbm_status lbm_output(lbm_solver *s, int32_t id, float **ptr, int64_t *count) {
   if (!s || !ptr || !count) return fail(LBM_ERR_ARG, "null argument");
-  if (id < 0 || id >= 5) return fail(LBM_ERR_ARG, "output id out of range (ux, uy, uz, p, vmag)");
+  if (id < 0 || id >= s->c.nout)
+    return fail(LBM_ERR_ARG, "output id out of range (ux, uy, uz, p, vmag; temp with heat)");
   *ptr = s->c.out[id];
   *count = (int64_t)s->c.out_dims[0] * s->c.out_dims[1] * s->c.out_dims[2];
   return LBM_OK;
@@ -852,6 +898,71 @@ lbm_status lbm_timing_read(lbm_solver *s, double out[7]) {
 lbm_status lbm_sync(lbm_solver *s) {
   LBM_HANDLE(s);
   return check_kernel_error(s);
+}
+
+lbm_status lbm_heat_field(lbm_solver *s, int32_t id, float **ptr) {
+  if (!s || !ptr) return fail(LBM_ERR_ARG, "null argument");
+  if (!s->c.cfg.heat) return fail(LBM_ERR_STATE, "the run has no heat");
+  if (id < 0 || id >= LBM_NUM_HEAT_FIELDS) return fail(LBM_ERR_ARG, "heat field id out of range (t_solid, q_solid, temp)");
+  *ptr = s->c.heat_fld[id];
+  return LBM_OK;
+}
+
+static lbm_status heat_copy(lbm_solver *s, void *host, int32_t dtype, int32_t where, bool in) {
+  if (!s || !host) return fail(LBM_ERR_ARG, "null argument");
+  if (!s->c.cfg.heat) return fail(LBM_ERR_STATE, "the run has no heat");
+  if (dtype != LBM_F32 && dtype != LBM_F64) return fail(LBM_ERR_ARG, "dtype must be LBM_F32 or LBM_F64");
+  if (where != LBM_HOST && where != LBM_DEVICE) return fail(LBM_ERR_ARG, "where must be LBM_HOST or LBM_DEVICE");
+  LBM_CUDA(cudaSetDevice(s->c.cfg.device));
+  LBM_CUDA(cudaDeviceSynchronize());
+  const size_t m = (size_t)7 * (size_t)s->c.n;
+  float *dev = s->c.g[s->c.g_cur];
+  if (dtype == LBM_F32) {
+    const cudaMemcpyKind kind = in ? (where == LBM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice)
+                                   : (where == LBM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice);
+    LBM_CUDA(in ? cudaMemcpy(dev, host, m * sizeof(float), kind) : cudaMemcpy(host, dev, m * sizeof(float), kind));
+    return LBM_OK;
+  }
+  // float64 values: converted on the host
+  std::vector<double> d(m);
+  std::vector<float> f(m);
+  if (in) {
+    LBM_CUDA(cudaMemcpy(d.data(), host, m * sizeof(double),
+                        where == LBM_HOST ? cudaMemcpyHostToHost : cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < m; ++i) f[i] = (float)d[i];
+    LBM_CUDA(cudaMemcpy(dev, f.data(), m * sizeof(float), cudaMemcpyHostToDevice));
+  } else {
+    LBM_CUDA(cudaMemcpy(f.data(), dev, m * sizeof(float), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < m; ++i) d[i] = (double)f[i];
+    LBM_CUDA(cudaMemcpy(host, d.data(), m * sizeof(double),
+                        where == LBM_HOST ? cudaMemcpyHostToHost : cudaMemcpyHostToDevice));
+  }
+  return LBM_OK;
+}
+
+lbm_status lbm_set_heat_populations(lbm_solver *s, const void *g, int32_t dtype, int32_t where) {
+  return heat_copy(s, const_cast<void *>(g), dtype, where, true);
+}
+
+lbm_status lbm_get_heat_populations(lbm_solver *s, void *g, int32_t dtype, int32_t where) {
+  return heat_copy(s, g, dtype, where, false);
+}
+
+lbm_status lbm_set_sink(lbm_solver *s, const double sink[8]) {
+  LBM_HANDLE(s);
+  if (!sink) return fail(LBM_ERR_ARG, "null sink");
+  lbm_config g = s->c.cfg;
+  for (int k = 0; k < 8; ++k) g.sink[k] = sink[k];
+  if (g.obstacle != LBM_HEATSINK) {
+    g.obstacle = LBM_HEATSINK;  // validate the sizes as a heat sink
+    lbm_status st = validate(g);
+    if (st != LBM_OK) return st;
+    for (int k = 0; k < 8; ++k) s->c.cfg.sink[k] = sink[k];
+    return LBM_OK;
+  }
+  double geo[7] = {g.ox, g.oy, g.oz, g.r, g.hx, g.hy, g.hz};
+  for (int k = 0; k < 8; ++k) s->c.cfg.sink[k] = sink[k];
+  return lbm_set_obstacle(s, LBM_HEATSINK, geo);
 }
 
 }  // extern "C"

@@ -82,13 +82,18 @@ __host__ __device__ constexpr float wq(int q) {
 constexpr double W_EXCESS = 1.4901161193847656e-08;
 
 enum { COLL_BGK = 0, COLL_TRT = 1, COLL_LES = 2 };
-enum { OBS_NONE = 0, OBS_CYL = 1, OBS_SPH = 2, OBS_BOX = 3 };
+enum { OBS_NONE = 0, OBS_CYL = 1, OBS_SPH = 2, OBS_BOX = 3, OBS_SINK = 4 };
 enum { SIDE_PERIODIC = 0, SIDE_SLIP = 1, SIDE_LID = 2 };
 
 struct Geo {
   int kind;
   float ox, oy, oz, r2, inv_r, hx, hy, hz;
   float r;
+  // heat sink (HeatSink, lbm.py:230-276): x range [sx0, sx1), z range [sz0,
+  // sz1), plate below y = sybase, fins below y = sytop every spitch cells in z
+  // (sthick thick) starting at z = iz0; duct walls at y = 0 and y = ny - 1
+  float sx0, sx1, sz0, sz1, sybase, sytop;
+  int iz0, sthick, spitch, ny;
 };
 
 // Everything a step launch needs, passed by value (__grid_constant__).
@@ -107,6 +112,7 @@ struct StepArgs {
   P wall_ox, wall_oy, wall_inv_r;     // cylinder axis and 1/r for the moving-wall term
   P omega_bgk, tau0, smag_c, magic;   // smag_c = 25.456 cs^2 (lbm.py:93)
   float *fld[13];
+  float4 *aux;            // temperature runs: (ux, uy, uz, tau) of every fluid cell, else null
   float2 *partials;       // NSUM compensated float pairs per block (report steps)
   int reach_lo[3], reach_hi[3];  // cells that may be solid or next to solid lie in this box
   int reach_any;                 // 0: no obstacle cell at all
@@ -129,6 +135,17 @@ inline Geo make_geo(const Cfg &g) {
   o.hx = (float)g.hx;
   o.hy = (float)g.hy;
   o.hz = (float)g.hz;
+  // sink = {x0, length, z0, width, base, fin_height, fin_thickness, fin_pitch}
+  o.sx0 = (float)g.sink[0];
+  o.sx1 = (float)(g.sink[0] + g.sink[1]);
+  o.sz0 = (float)g.sink[2];
+  o.sz1 = (float)(g.sink[2] + g.sink[3]);
+  o.sybase = (float)(1.0 + g.sink[4]);
+  o.sytop = (float)(1.0 + g.sink[4] + g.sink[5]);
+  o.iz0 = (int)g.sink[2];
+  o.sthick = (int)g.sink[6];
+  o.spitch = g.sink[7] >= 1.0 ? (int)g.sink[7] : 1;
+  o.ny = g.ny;
   return o;
 }
 
@@ -198,7 +215,18 @@ __host__ __device__ constexpr T rest_value(int q) {
 // product and sum rounded separately (no fused multiply-add), so the mask is
 // reproducible on the host bit for bit (lbm.py:150-153, 177-182, 207-211).
 
+// HeatSink.sink (lbm.py:250-261): the base plate and fins
+__host__ __device__ __forceinline__ bool sink(const Geo &g, int x, int y, int z) {
+  if (g.kind != OBS_SINK) return false;
+  const float fx = (float)x, fy = (float)y, fz = (float)z;
+  const bool inside = fx >= g.sx0 && fx < g.sx1 && fz >= g.sz0 && fz < g.sz1 && fy >= 1.0f;
+  int m = (z - g.iz0) % g.spitch;
+  m += m < 0 ? g.spitch : 0;
+  return inside && (fy < g.sybase || (fy < g.sytop && m < g.sthick));
+}
+
 __device__ __forceinline__ bool solid(const Geo &g, int x, int y, int z) {
+  if (g.kind == OBS_SINK) return y <= 0 || y >= g.ny - 1 || sink(g, x, y, z);
   const float fx = (float)x, fy = (float)y, fz = (float)z;
   if (g.kind == OBS_CYL) {
     const float dx = __fsub_rn(fx, g.ox), dy = __fsub_rn(fy, g.oy);
@@ -350,14 +378,16 @@ __device__ __forceinline__ void relax_bgk(T v[Q], T om, const T A[9], const T B[
 
 // Relax the values v[] in place: BGK (lbm.py:60-69), TRT + Smagorinsky
 // (lbm.py:96-123), LES-BGK (lbm.py:126-139).
+// Returns the relaxation time (the D3Q7 temperature block's subgrid
+// diffusivity uses it, lbm.py:299-301).
 template <typename T, int COLL, bool DEV>
-__device__ __forceinline__ void collide(T v[Q], const Moments<T> &m, const Pairs<T> &pr, T omega_bgk, T tau0,
-                                        T smag_c, T magic) {
+__device__ __forceinline__ T collide(T v[Q], const Moments<T> &m, const Pairs<T> &pr, T omega_bgk, T tau0,
+                                     T smag_c, T magic) {
   T A[9], B[9], eq0;
   eq_pairs<T, DEV>(rv_of<T, DEV>(m), m.rho, m.ux, m.uy, m.uz, A, B, eq0);
   if (COLL == COLL_BGK) {
     relax_bgk<T>(v, omega_bgk, A, B, eq0);
-    return;
+    return tau0;
   }
   // Smagorinsky relaxation time from the non-equilibrium stress (lbm.py:72-93)
   const T uxx = m.ux * m.ux, uyy = m.uy * m.uy, uzz = m.uz * m.uz, usq = uxx + uyy + uzz;
@@ -375,7 +405,7 @@ __device__ __forceinline__ void collide(T v[Q], const Moments<T> &m, const Pairs
   const T tau = T(0.5) * (tau0 + sqrt_fast<T>(tau0 * tau0 + smag_c * pi * rcp_fast<T>(m.rho)));
   if (COLL == COLL_LES) {
     relax_bgk<T>(v, rcp_fast<T>(tau), A, B, eq0);
-    return;
+    return tau;
   }
   // TRT: even/odd parts relaxed at omega+ = 1/tau, omega- = 1/(magic/(tau-1/2)+1/2)
   const T hp = T(0.5) * rcp_fast<T>(tau);
@@ -391,6 +421,7 @@ __device__ __forceinline__ void collide(T v[Q], const Moments<T> &m, const Pairs
     v[q] = v[q] - sym - anti;
     v[q + 1] = v[q + 1] - sym + anti;
   }
+  return tau;
 }
 
 // Sponge blend toward (1, u0*fluid, 0, 0) (lbm.py:446-456):
@@ -699,7 +730,8 @@ __device__ __forceinline__ void fast_finish(const StepArgs<S> &a, int x, int y, 
   Pairs<T> pr;
   const Moments<T> mo = moments<T, DEV>(d, !here, pr);
   if (!here) {
-    collide<T, COLL, DEV>(d, mo, pr, a.omega_bgk, a.tau0, a.smag_c, a.magic);
+    const T tau = collide<T, COLL, DEV>(d, mo, pr, a.omega_bgk, a.tau0, a.smag_c, a.magic);
+    if (a.aux) a.aux[idx] = make_float4((float)mo.ux, (float)mo.uy, (float)mo.uz, (float)tau);
     const T t = fmax(T(0), (T(x) - a.sponge_start) * a.inv_sponge_len);
     const T sigma = a.sponge_strength * t * t;
     if (sigma != T(0)) sponge<T, DEV>(d, mo, sigma, a.u0);
@@ -813,7 +845,8 @@ __device__ __forceinline__ void general_cell(const StepArgs<S> &a, int x, int y,
   Pairs<T> pr;
   const Moments<T> m = moments<T, DEV>(d, !here, pr);
   if (!here) {
-    collide<T, COLL, DEV>(d, m, pr, a.omega_bgk, a.tau0, a.smag_c, a.magic);
+    const T tau = collide<T, COLL, DEV>(d, m, pr, a.omega_bgk, a.tau0, a.smag_c, a.magic);
+    if (a.aux) a.aux[idx] = make_float4((float)m.ux, (float)m.uy, (float)m.uz, (float)tau);
     const T t = fmax(T(0), (T(x) - a.sponge_start) * a.inv_sponge_len);
     const T sigma = a.sponge_strength * t * t;
     if (sigma != T(0)) sponge<T, DEV>(d, m, sigma, a.u0);

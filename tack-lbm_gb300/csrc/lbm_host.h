@@ -34,7 +34,13 @@ struct Ctx {
   double omega_rot;
   int out_stride;            // output grid subsampling (1: aliases fld)
   int out_dims[3];
-  float *out[5];             // coarse ux, uy, uz, p, vmag (owned when out_stride > 1)
+  int nout;                  // output fields: 5, or 6 with temperature
+  float *out[LBM_MAX_OUTPUTS];  // coarse ux, uy, uz, p, vmag, temp (owned when out_stride > 1)
+  // D3Q7 temperature (cfg.heat): A/B populations, the flow's per-cell moments, fields
+  float *g[2];
+  int g_cur;                 // g[g_cur] holds the current temperature populations
+  float4 *aux;               // (ux, uy, uz, tau) per fluid cell, written by the flow step
+  float *heat_fld[LBM_NUM_HEAT_FIELDS];
   // optional kernel timing: events around the bulk and generic launches
   cudaEvent_t *ev;           // 3 events per step in a ring (bulk start, bulk end/generic start, generic end)
   int ev_cap, ev_used;
@@ -68,6 +74,9 @@ template <typename S> cudaError_t launch_warp_masks(const Ctx &c, cudaStream_t s
 cudaError_t launch_finalize(const Ctx &c, int64_t rows, cudaStream_t st);
 cudaError_t launch_mask(const Ctx &c, uint8_t *dst_dev, cudaStream_t st);
 cudaError_t launch_coarsen(const Ctx &c, cudaStream_t st);
+cudaError_t launch_heat(const Ctx &c, bool report, cudaStream_t st);
+// the full-resolution field output k shows (fld[k], or the temperature)
+inline float *output_source(const Ctx &c, int k) { return k < 5 ? c.fld[k] : c.heat_fld[LBM_TEMP]; }
 
 // message returned by lbm_last_error() on this thread
 void set_last_error(const std::string &msg);

@@ -39,6 +39,7 @@ StepArgs<S> make_args(const Ctx &c) {
   a.smag_c = (P)(25.456 * g.cs * g.cs);
   a.magic = (P)g.magic;
   for (int k = 0; k < LBM_NUM_FIELDS; ++k) a.fld[k] = c.fld[k];
+  a.aux = c.cfg.heat ? c.aux : nullptr;
   a.partials = c.partials;
   for (int k = 0; k < 3; ++k) {
     a.reach_lo[k] = c.reach_lo[k];

@@ -38,6 +38,13 @@ CX = [0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0]
 CY = [0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -1]
 CZ = [0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1]
 W = [1 / 3] + [1 / 18] * 6 + [1 / 36] * 12
+
+# D3Q7 for temperature: rest plus the six faces, c_s^2 = 1/4 (lbm.py:20-25)
+CX7 = [0, 1, -1, 0, 0, 0, 0]
+CY7 = [0, 0, 0, 1, -1, 0, 0]
+CZ7 = [0, 0, 0, 0, 0, 1, -1]
+W7 = [1 / 4] + [1 / 8] * 6
+OPP7 = [0, 2, 1, 4, 3, 6, 5]
 FIELDS = N.FIELDS
 
 
@@ -154,6 +161,23 @@ class NoObstacle:
         return [0.0] * 7
 
 
+class HeatSink:
+    """A finned heat sink on the floor of a duct (lbm.py:230-276): base plate and
+    fins along x, duct walls at y = 0 and y = ny - 1. Sizes in lattice cells."""
+
+    code = N.HEATSINK
+
+    def __init__(self, ny, x0, length, z0, width, base, fin_height, fin_thickness, fin_pitch):
+        self.ny = ny
+        self.params = [float(v) for v in (x0, length, z0, width, base, fin_height, fin_thickness, fin_pitch)]
+
+    def geometry(self):
+        return [0.0] * 7
+
+    def sink_params(self):
+        return list(self.params)
+
+
 class PeriodicY:
     code = N.PERIODIC
 
@@ -196,9 +220,29 @@ class Flow:
 
 
 class NoHeat:
-    """The disabled thermal variant (lbm.py:282-308); the D3Q7 block is not built."""
+    """The disabled thermal variant (lbm.py:282-308)."""
 
     enabled = 0
+    Q = 7
+    pr_t = 0.85
+
+    def __init__(self, arrays=None):
+        self.arrays = arrays or {}
+        self.alpha = 0.0
+        self.nu = 0.0
+
+
+class Heat(NoHeat):
+    """D3Q7 temperature (lbm.py:311-319): ``arrays`` holds ``t_solid``,
+    ``q_solid`` and ``temp`` (length n); ``alpha`` is the molecular diffusivity,
+    ``nu`` the viscosity the subgrid diffusivity subtracts."""
+
+    enabled = 1
+
+    def __init__(self, arrays, alpha, nu):
+        super().__init__(arrays)
+        self.alpha = alpha
+        self.nu = nu
 
 
 class Quiet:
@@ -259,7 +303,7 @@ class ManagedArray:
 COLLISIONS = {"bgk": BGK, "trt": TRT, "les": SmagorinskyLES}
 
 
-def _config(lat, phys, geo, flow, storage="f32", device=0):
+def _config(lat, phys, geo, flow, storage="f32", device=0, heat=None):
     c = N.Config()
     c.nx, c.ny, c.nz = lat.nx, lat.ny, lat.nz
     c.collision = phys.code
@@ -277,6 +321,12 @@ def _config(lat, phys, geo, flow, storage="f32", device=0):
     c.u_lid = getattr(flow.side, "u_lid", 0.0)
     c.omega_rot = flow.rotation()
     c.device = device
+    if hasattr(geo, "sink_params"):
+        c.sink[:] = geo.sink_params()
+    if heat is not None and getattr(heat, "enabled", 0):
+        c.heat = 1
+        c.alpha = float(heat.alpha)
+        c.heat_nu = float(heat.nu)
     return c
 
 
@@ -291,15 +341,22 @@ def lbm_init(lat, geo, flow, f, seed_amp, storage="f32", device=0):
     return out
 
 
+def _heat_view(h, k, n):
+    ptr = ctypes.c_void_p()
+    h.call("lbm_heat_field", k, ctypes.byref(ptr))
+    return np.ctypeslib.as_array((ctypes.c_float * n).from_address(ptr.value))
+
+
 def lbm_step(lat, phys, geo, flow, diag, f_in, f_out, heat=None, g_in=None, g_out=None,
              storage="f32", device=0):
     """One step from host populations ``f_in`` into ``f_out`` (the reference's
     kernel signature, lbm.py:397-398). With a ``Report`` diag the 13 fields of
-    ``diag.fields`` are read (previous ux, uy, uz, p) and rewritten.
-    The thermal block (``heat``) is not supported and must be disabled."""
-    if heat is not None and getattr(heat, "enabled", 0):
-        raise NotImplementedError("the D3Q7 thermal block is not part of this solver")
-    h = N.Handle(_config(lat, phys, geo, flow, storage, device))
+    ``diag.fields`` are read (previous ux, uy, uz, p) and rewritten. With an
+    enabled ``Heat`` the temperature populations go from ``g_in`` to ``g_out``
+    (7*n), ``heat.arrays["t_solid"]`` is read and, on report steps,
+    ``temp`` is written and ``q_solid`` accumulated (lbm.py:457-492)."""
+    heat_on = heat is not None and getattr(heat, "enabled", 0)
+    h = N.Handle(_config(lat, phys, geo, flow, storage, device, heat))
     src = np.ascontiguousarray(_host(f_in), dtype=np.float64).reshape(-1)
     h.call("lbm_set_populations", src.ctypes.data_as(ctypes.c_void_p), N.F64, N.HOST)
     report = bool(getattr(diag, "enabled", 0))
@@ -307,6 +364,15 @@ def lbm_step(lat, phys, geo, flow, diag, f_in, f_out, heat=None, g_in=None, g_ou
         for k, name in enumerate(N.FIELDS):
             v = np.ascontiguousarray(_host(diag.fields[name]), dtype=np.float32)
             h.call("lbm_set_field", k, v.ctypes.data_as(ctypes.c_void_p))
+    if heat_on:
+        gsrc = np.ascontiguousarray(_host(g_in), dtype=np.float64).reshape(-1)
+        h.call("lbm_set_heat_populations", gsrc.ctypes.data_as(ctypes.c_void_p), N.F64, N.HOST)
+        h.call("lbm_sync")
+        _heat_view(h, 0, lat.n)[...] = np.asarray(_host(heat.arrays["t_solid"]), np.float32).reshape(-1)
+    if heat_on and report:
+        # the reference accumulates into q_solid (the caller zeroes it); the
+        # library zeroes it first, so add the caller's values back afterwards
+        q_before = np.asarray(_host(heat.arrays["q_solid"]), np.float32).reshape(-1).copy()
     h.call("lbm_step", int(report), None)
     out = _host(f_out)
     buf = np.empty(19 * lat.n, np.float64)
@@ -319,6 +385,15 @@ def lbm_step(lat, phys, geo, flow, diag, f_in, f_out, heat=None, g_in=None, g_ou
             h.call("lbm_field", k, ctypes.byref(ptr))
             vals = np.ctypeslib.as_array((ctypes.c_float * lat.n).from_address(ptr.value))
             _host(diag.fields[name])[...] = vals
+    if heat_on:
+        gbuf = np.empty(7 * lat.n, np.float64)
+        h.call("lbm_get_heat_populations", gbuf.ctypes.data_as(ctypes.c_void_p), N.F64, N.HOST)
+        gout = _host(g_out)
+        gout[...] = gbuf.reshape(gout.shape).astype(gout.dtype, copy=False)
+        if report:
+            h.call("lbm_sync")
+            _host(heat.arrays["temp"])[...] = _heat_view(h, 2, lat.n)
+            _host(heat.arrays["q_solid"])[...] = _heat_view(h, 1, lat.n) + q_before
     return out
 
 
@@ -335,8 +410,6 @@ class Solver:
                  vertical="periodic", cs=None, obstacle_center=None, obstacle_size=None,
                  sponge_start=None, sponge_planes=None, sponge_strength=1.0, u_lid=0.0,
                  init="wave", seed=0, rho_sigma=1e-3, u_noise=0.01, kernel="auto"):
-        if heat:
-            raise NotImplementedError("heat=True (the D3Q7 thermal block) is not part of this solver")
         self.device_index = 0 if device in ("cuda", None) else int(str(device).split(":")[-1])
         self.lateral = lateral
         self.vertical_policy = vertical
@@ -345,9 +418,8 @@ class Solver:
         self.lat = D3Q19(nx, ny, nz)
         self.u0, self.diameter = u0, diameter
         self.step_count = 0
-        self.heat_enabled = False
+        self.heat_enabled = bool(heat)
         self.prandtl = prandtl
-        self._setup_heat(nx * ny * nz)
         self._cs = cs
         self._obstacle_center = obstacle_center
         self._obstacle_size = obstacle_size
@@ -359,10 +431,16 @@ class Solver:
                          np.zeros(1, np.float32), side, vert)
         self.set_obstacle(obstacle, _apply=False)
         self.set_physics(collision, reynolds, _apply=False)
-        cfg = _config(self.lat, self.phys, self.geo, self.flow, storage, self.device_index)
+        n = self.lat.n
+        if self.heat_enabled:
+            # Heat(arrays, nu / prandtl, nu) at construction (lbm.py:596-599)
+            self.heat = Heat({}, self.nu / self.prandtl, self.nu)
+        else:
+            self.heat = NoHeat()
+        cfg = _config(self.lat, self.phys, self.geo, self.flow, storage, self.device_index, self.heat)
         cfg.flags = {"auto": 0, "bulkcopy": N.FLAG_BULKCOPY, "simt": N.FLAG_SIMT}[kernel]
         self._h = N.Handle(cfg)
-        n = self.lat.n
+        self._setup_heat(n)
         self.fields = {}
         for k, name in enumerate(FIELDS):
             ptr = ctypes.c_void_p()
@@ -372,10 +450,12 @@ class Solver:
         self.out_dims = tuple((d + stride - 1) // stride for d in (nx, ny, nz))
         self._h.call("lbm_set_output_stride", int(stride))
         self.output = {}
-        for k, name in enumerate(self.OUTPUT):
+        outputs = self.OUTPUT + (("temp",) if self.heat_enabled else ())
+        for k, name in enumerate(outputs):
             ptr, cnt = ctypes.c_void_p(), ctypes.c_int64()
             self._h.call("lbm_output", k, ctypes.byref(ptr), ctypes.byref(cnt))
-            self.output[name] = self.fields[name] if stride == 1 else ManagedArray.view(ptr.value, cnt.value, self._h)
+            full = self.heat_fields[name] if name == "temp" else self.fields.get(name)
+            self.output[name] = full if stride == 1 else ManagedArray.view(ptr.value, cnt.value, self._h)
         if init == "wave":
             self._h.call("lbm_init", 0.05)
         elif init == "random":
@@ -386,10 +466,35 @@ class Solver:
         self.step_count = 0
 
     def _setup_heat(self, n):
-        """Thermal state of a solver without heat (lbm.py:586-600)."""
+        """The temperature fields t_solid, q_solid, temp (lbm.py:586-600): managed
+        arrays of n floats when the run has heat, empty otherwise."""
         self.heat_fields = {}
-        self.heat = NoHeat()
-        self.g = [None, None]
+        if self.heat_enabled:
+            for k, name in enumerate(N.HEAT_FIELDS):
+                ptr = ctypes.c_void_p()
+                self._h.call("lbm_heat_field", k, ctypes.byref(ptr))
+                self.heat_fields[name] = ManagedArray.view(ptr.value, n, self._h)
+            self.heat.arrays = {k: v.numpy for k, v in self.heat_fields.items()}
+
+    def set_wall_temperature(self, value):
+        """Fill every solid voxel's temperature (lbm.py:602-604)."""
+        self.sync()
+        self.heat_fields["t_solid"].numpy[:] = value
+
+    @property
+    def g(self):
+        """The current temperature populations g[q*n + idx] (7*n), in a one-element list."""
+        if not self.heat_enabled:
+            return [None]
+        out = np.empty(7 * self.lat.n, np.float32)
+        self._h.call("lbm_get_heat_populations", out.ctypes.data_as(ctypes.c_void_p), N.F32, N.HOST)
+        return [out]
+
+    def set_heat_populations(self, g):
+        src = np.ascontiguousarray(_host(g), dtype=np.float64).reshape(-1)
+        if src.size != 7 * self.lat.n:
+            raise ValueError("temperature populations must hold 7*n values")
+        self._h.call("lbm_set_heat_populations", src.ctypes.data_as(ctypes.c_void_p), N.F64, N.HOST)
 
     # -- composition ------------------------------------------------------
     def set_physics(self, collision, reynolds, _apply=True):
@@ -416,12 +521,18 @@ class Solver:
         elif kind == "box":
             hx, hy, hz = (r, r, 0.3 * nz) if size is None else size
             geo = Box(x0, y0, z0, hx, hy, hz)
+        elif kind == "heatsink":
+            d = self.diameter
+            geo = HeatSink(ny, int(0.2 * nx), int(0.3 * nx), int(0.125 * nz), int(0.75 * nz), round(d / 2),
+                           int(0.45 * ny), round(d / 3), round(d))
         elif kind == "none":
             geo = NoObstacle()
         else:
             raise KeyError(kind)
         self.geo = geo
         if _apply:
+            if kind == "heatsink":
+                self._h.call("lbm_set_sink", (ctypes.c_double * 8)(*geo.sink_params()))
             g = (ctypes.c_double * 7)(*geo.geometry())
             self._h.call("lbm_set_obstacle", geo.code, g)
 

@@ -13,7 +13,7 @@ LIB_PATH = os.path.join(HERE, "liblbm_gb300.so")
 
 OK, ERR_ARG, ERR_CUDA, ERR_NONFINITE, ERR_STATE = range(5)
 BGK, TRT, LES = 0, 1, 2
-NO_OBSTACLE, CYLINDER, SPHERE, BOX = 0, 1, 2, 3
+NO_OBSTACLE, CYLINDER, SPHERE, BOX, HEATSINK = 0, 1, 2, 3, 4
 PERIODIC, SLIP, LID = 0, 1, 2
 F32, F16, BF16, F64 = 0, 1, 2, 3
 HOST, DEVICE = 0, 1
@@ -23,7 +23,9 @@ FIELDS = ("ux", "uy", "uz", "p", "vmag", "r_rho", "r_ux", "r_uy", "r_uz", "r_ke"
 MONITORS = ("continuity", "momentum_x", "momentum_y", "momentum_z", "energy", "drag", "lift")
 STORAGE = {"f32": F32, "f16": F16, "bf16": BF16, "f64": F64}
 COLLISION = {"bgk": BGK, "trt": TRT, "les": LES}
-OBSTACLE = {"none": NO_OBSTACLE, "cylinder": CYLINDER, "sphere": SPHERE, "box": BOX}
+OBSTACLE = {"none": NO_OBSTACLE, "cylinder": CYLINDER, "sphere": SPHERE, "box": BOX, "heatsink": HEATSINK}
+HEAT_FIELDS = ("t_solid", "q_solid", "temp")
+OUT_TEMP = 5
 SIDE = {"periodic": PERIODIC, "slip": SLIP, "lid": LID}
 
 
@@ -48,6 +50,9 @@ class Config(ctypes.Structure):
         ("u0", ctypes.c_double), ("sponge_start", ctypes.c_double), ("sponge_strength", ctypes.c_double),
         ("u_lid", ctypes.c_double), ("omega_rot", ctypes.c_double),
         ("device", ctypes.c_int32), ("flags", ctypes.c_int32),
+        ("sink", ctypes.c_double * 8),
+        ("heat", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("alpha", ctypes.c_double), ("heat_nu", ctypes.c_double),
     ]
 
 
@@ -100,6 +105,12 @@ _SIGNATURES = {
                                              ctypes.c_void_p, ctypes.c_void_p]),
     "lbm_managed_alloc": (ctypes.c_int, [ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
     "lbm_managed_free": (ctypes.c_int, [ctypes.c_void_p]),
+    "lbm_set_sink": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
+    "lbm_heat_field": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]),
+    "lbm_set_heat_populations": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                                ctypes.c_int32]),
+    "lbm_get_heat_populations": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                                ctypes.c_int32]),
     "lbm_adj_create": (ctypes.c_int, [ctypes.POINTER(AdjConfig), ctypes.POINTER(ctypes.c_void_p)]),
     "lbm_adj_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "lbm_adj_set_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),

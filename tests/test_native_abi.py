@@ -34,14 +34,17 @@ def test_every_declared_symbol_is_exported(N):
 
 
 def test_abi_version(N):
-    assert N.load().lbm_abi_version() == 1
+    assert N.load().lbm_abi_version() == 2
 
 
 def test_config_layout(N):
-    # 8 int32, 15 doubles, 2 int32 (include/lbm_gb300.h struct lbm_config)
-    assert ctypes.sizeof(N.Config) == 8 * 4 + 15 * 8 + 2 * 4
+    # 8 int32, 15 doubles, 2 int32, 8 doubles, 2 int32, 2 doubles
+    # (include/lbm_gb300.h struct lbm_config)
+    assert ctypes.sizeof(N.Config) == 8 * 4 + 15 * 8 + 2 * 4 + 8 * 8 + 2 * 4 + 2 * 8
     assert N.Config.nu.offset == 32
     assert N.Config.device.offset == 32 + 15 * 8
+    assert N.Config.sink.offset == 32 + 15 * 8 + 8
+    assert N.Config.heat_nu.offset == 32 + 15 * 8 + 8 + 64 + 8 + 8
 
 
 def base_config(N):
@@ -55,11 +58,15 @@ def base_config(N):
 
 @pytest.mark.parametrize("field,value", [
     ("collision", 7), ("obstacle", 9), ("lateral", 5), ("vertical", 2), ("storage", 11),
-    ("nx", 0), ("nu", 0.0), ("nu", float("nan")), ("cs", -1.0), ("u0", float("inf"))])
+    ("nx", 0), ("nu", 0.0), ("nu", float("nan")), ("cs", -1.0), ("u0", float("inf")),
+    ("alpha", -1.0), ("storage_with_heat", 1)])
 def test_invalid_config_is_an_argument_error(N, field, value):
     """Unknown models and bad sizes are rejected before any device work
     (the reference raises KeyError, lbm.py:616, lbm.py:632-637)."""
     c = base_config(N)
+    if field in ("alpha", "storage_with_heat"):
+        c.heat = 1
+        field = "storage" if field == "storage_with_heat" else field
     setattr(c, field, value)
     ptr = ctypes.c_void_p()
     status = N.load().lbm_create(ctypes.byref(c), ctypes.byref(ptr))
