@@ -373,8 +373,7 @@ def main():
             s.step()
         s.step(report=True)
         m = s.monitors(E2E_INTERVAL)
-        for k in s.OUTPUT:
-            np.copyto(host_out[k], s.output[k].numpy)
+        s.read_output(host_out)
         s.set_actuation(omega)
         return m
 
@@ -399,7 +398,8 @@ def main():
         "e2e": {"value": e2e_value, "unit": "GLUPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "api": (f"tack-lbm's run loop: per {E2E_INTERVAL} steps {E2E_INTERVAL - 1} x Solver.step(), "
                         f"Solver.step(report=True), Solver.monitors() (output grid stride {E2E_STRIDE}), "
-                        "the 5 output fields copied to pinned host memory, Solver.set_actuation()"),
+                        "Solver.read_output() of the 5 output fields into pinned host memory, "
+                        "Solver.set_actuation()"),
                 "steps": e2e_steps, "ms_per_step": e2e_wall / e2e_steps * 1e3},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs (burst copy)",

@@ -182,6 +182,12 @@ lbm_status lbm_set_output_stride(lbm_solver *s, int32_t stride);
 /* Managed pointer to output field `id` (LBM_UX .. LBM_VMAG, LBM_OUT_TEMP with heat)
  * and its point count. */
 lbm_status lbm_output(lbm_solver *s, int32_t id, float **ptr, int64_t *count);
+/* Copy output field `id` into `host` (its point count of floats; pinned host memory
+ * makes it an asynchronous copy-engine transfer) on `stream`, ordered after the
+ * steps and lbm_update_output on that stream. For consumers that want a host copy
+ * rather than reading the managed field in place. (No reference counterpart.) */
+lbm_status lbm_read_output(lbm_solver *s, int32_t id, float *host, void *stream);
+
 /* Refresh the output fields from the full-resolution ones: the coarsen kernel
  * (lbm.py:516-522) for every output field (Solver.update_output, lbm.py:606-611). */
 lbm_status lbm_update_output(lbm_solver *s, void *stream);

@@ -965,4 +965,14 @@ lbm_status lbm_set_sink(lbm_solver *s, const double sink[8]) {
   return lbm_set_obstacle(s, LBM_HEATSINK, geo);
 }
 
+lbm_status lbm_read_output(lbm_solver *s, int32_t id, float *host, void *stream) {
+  LBM_HANDLE(s);
+  if (!host) return fail(LBM_ERR_ARG, "null host buffer");
+  if (id < 0 || id >= s->c.nout)
+    return fail(LBM_ERR_ARG, "output id out of range (ux, uy, uz, p, vmag; temp with heat)");
+  const size_t m = (size_t)s->c.out_dims[0] * s->c.out_dims[1] * s->c.out_dims[2];
+  LBM_CUDA(cudaMemcpyAsync(host, s->c.out[id], m * sizeof(float), cudaMemcpyDefault, (cudaStream_t)stream));
+  return LBM_OK;
+}
+
 }  // extern "C"

@@ -565,6 +565,18 @@ class Solver:
     def update_output(self):
         self._h.call("lbm_update_output", None)
 
+    def read_output(self, out):
+        """Copy the output fields into the host arrays ``out[name]`` (float32,
+        C-contiguous, ideally pinned) with one copy-engine transfer each, then
+        wait for them: a host copy instead of reading the managed fields in place."""
+        for k, name in enumerate(self.output):
+            if name in out:
+                a = out[name]
+                if a.dtype != np.float32 or not a.flags.c_contiguous or a.size != self.output[name].numpy.size:
+                    raise ValueError(f"out[{name!r}] must be a C-contiguous float32 array of the output size")
+                self._h.call("lbm_read_output", k, a.ctypes.data_as(ctypes.c_void_p), None)
+        self.sync()
+
     def monitors(self, interval):
         self.update_output()
         out = (ctypes.c_double * 7)()

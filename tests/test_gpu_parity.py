@@ -326,9 +326,12 @@ def test_output_stride(G):
         s.step()
     s.step(report=True)
     s.monitors(4)
+    host = {name: np.full(14 * 7 * 4, np.nan, np.float32) for name in s.OUTPUT}
+    s.read_output(host)
     for name in s.OUTPUT:
         full = s.fields[name].numpy.reshape(10, 20, 40)
         assert np.array_equal(s.output[name].numpy.reshape(4, 7, 14), full[::3, ::3, ::3]), name
+        assert np.array_equal(host[name], s.output[name].numpy), name
 
 
 def test_nonfinite_monitors_reported(G):
