@@ -192,6 +192,20 @@ lbm_status lbm_read_output(lbm_solver *s, int32_t id, float *host, void *stream)
  * (lbm.py:516-522) for every output field (Solver.update_output, lbm.py:606-611). */
 lbm_status lbm_update_output(lbm_solver *s, void *stream);
 
+/* Velocity gradient on the output grid (derived.py:52-89): jac receives 9 floats
+ * per output point, jac[9 p + 3 c + d] = d u_c / d x_d, central differences and
+ * one-sided at the grid's faces, scaled by inv_h (the reference passes
+ * diameter / stride, derived.py:101-103). Reads the output fields as the last
+ * lbm_update_output left them. jac: device or managed memory. */
+lbm_status lbm_velocity_gradient(lbm_solver *s, float *jac, double inv_h, void *stream);
+
+/* |curl u| and the Q-criterion -1/2 J_ij J_ji from such a gradient (the default
+ * derived fields, derived.py:27-30), one value per output point (at_cells = 0)
+ * or per cell centre (at_cells = 1: (mx-1)(my-1)(mz-1) values from the mean of
+ * the eight corner gradients). Either output may be NULL. */
+lbm_status lbm_vorticity_q(lbm_solver *s, const float *jac, float *vorticity, float *q, int32_t at_cells,
+                           void *stream);
+
 /* Overwrite one diagnostic field from a buffer of n floats (host or managed). */
 lbm_status lbm_set_field(lbm_solver *s, int32_t id, const float *host);
 

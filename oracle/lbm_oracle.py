@@ -502,3 +502,39 @@ def weight_err(a, b):
     """max |a - b| / w_q over all populations: the parity yardstick of the tests."""
     d = np.abs(np.asarray(a, np.float64).reshape(19, -1) - np.asarray(b, np.float64).reshape(19, -1))
     return float((d / W[:, None]).max())
+
+
+# ---------------------------------------------------------------------------
+# Derived fields on the output grid (derived.py:52-89): the velocity gradient
+# by central differences, one-sided at the grid's faces, and the default
+# fields |curl u| and Q = -1/2 J_ij J_ji (derived.py:27-30).
+
+def velocity_gradient(ux, uy, uz, dims, inv_h):
+    """(m, 3, 3) array, [p, c, d] = d u_c / d x_d at output point p."""
+    mx, my, mz = dims
+    u = [np.asarray(a, np.float64).reshape(mz, my, mx) for a in (ux, uy, uz)]
+    out = np.zeros((mz, my, mx, 3, 3))
+    for d, axis, n in ((0, 2, mx), (1, 1, my), (2, 0, mz)):
+        idx = np.arange(n)
+        lo, hi = np.maximum(idx - 1, 0), np.minimum(idx + 1, n - 1)
+        span = (hi - lo).astype(np.float64)
+        scale = np.where(span > 0, inv_h / np.where(span > 0, span, 1.0), 0.0)
+        shape = [1, 1, 1]
+        shape[axis] = n
+        for c in range(3):
+            diff = np.take(u[c], hi, axis=axis) - np.take(u[c], lo, axis=axis)
+            out[..., c, d] = diff * scale.reshape(shape)
+    return out.reshape(-1, 3, 3)
+
+
+def vorticity_q(jac, dims, at_cells=False):
+    """|curl u| and Q from a point gradient, at points or at cell centres (mean of
+    the eight corner gradients)."""
+    mx, my, mz = dims
+    g = np.asarray(jac, np.float64).reshape(mz, my, mx, 3, 3)
+    if at_cells:
+        g = sum(g[k:mz - 1 + k, j:my - 1 + j, i:mx - 1 + i] for k in (0, 1) for j in (0, 1) for i in (0, 1)) / 8.0
+    g = g.reshape(-1, 3, 3)
+    w = np.stack([g[:, 2, 1] - g[:, 1, 2], g[:, 0, 2] - g[:, 2, 0], g[:, 1, 0] - g[:, 0, 1]], 1)
+    q = -0.5 * np.einsum("pab,pba->p", g, g)
+    return np.linalg.norm(w, axis=1), q

@@ -975,4 +975,21 @@ lbm_status lbm_read_output(lbm_solver *s, int32_t id, float *host, void *stream)
   return LBM_OK;
 }
 
+lbm_status lbm_velocity_gradient(lbm_solver *s, float *jac, double inv_h, void *stream) {
+  LBM_HANDLE(s);
+  if (!jac) return fail(LBM_ERR_ARG, "null gradient buffer");
+  if (!std::isfinite(inv_h)) return fail(LBM_ERR_ARG, "inv_h must be finite");
+  LBM_CUDA(lbmh::launch_jacobian(s->c, jac, (float)inv_h, (cudaStream_t)stream));
+  return LBM_OK;
+}
+
+lbm_status lbm_vorticity_q(lbm_solver *s, const float *jac, float *vorticity, float *q, int32_t at_cells,
+                           void *stream) {
+  LBM_HANDLE(s);
+  if (!jac) return fail(LBM_ERR_ARG, "null gradient buffer");
+  if (at_cells != 0 && at_cells != 1) return fail(LBM_ERR_ARG, "at_cells must be 0 or 1");
+  LBM_CUDA(lbmh::launch_vortq(s->c, jac, vorticity, q, at_cells, (cudaStream_t)stream));
+  return LBM_OK;
+}
+
 }  // extern "C"

@@ -105,6 +105,9 @@ _SIGNATURES = {
                                              ctypes.c_void_p, ctypes.c_void_p]),
     "lbm_managed_alloc": (ctypes.c_int, [ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
     "lbm_managed_free": (ctypes.c_int, [ctypes.c_void_p]),
+    "lbm_velocity_gradient": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p]),
+    "lbm_vorticity_q": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_int32, ctypes.c_void_p]),
     "lbm_read_output": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]),
     "lbm_set_sink": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
     "lbm_heat_field": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]),

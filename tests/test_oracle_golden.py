@@ -141,3 +141,19 @@ def test_heat_step_golden(case):
         assert np.abs(heat["q_solid"] - case["q_solid"]).max() < 1e-11
         for k in O.FIELDS:
             assert np.abs(fields[k] - case["fields"][k]).max() < 1e-12, k
+
+
+def test_velocity_gradient_of_a_linear_field():
+    """The derived-field gradient (derived.py:52-89) is exact for a linear field
+    inside the grid and one-sided (still exact) at its faces; vorticity and Q of
+    u = (a y, 0, 0): |curl u| = |a|, Q = 0 (pure shear)."""
+    mx, my, mz = 7, 5, 4
+    z, y, x = np.meshgrid(np.arange(mz), np.arange(my), np.arange(mx), indexing="ij")
+    ux, uy, uz = 0.3 * x + 0.2 * y, -0.1 * z, 0.05 * x
+    g = O.velocity_gradient(ux.ravel(), uy.ravel(), uz.ravel(), (mx, my, mz), 2.0)
+    want = 2.0 * np.array([[0.3, 0.2, 0.0], [0.0, 0.0, -0.1], [0.05, 0.0, 0.0]])
+    assert np.allclose(g, want[None], atol=1e-12)
+    gs = O.velocity_gradient((0.4 * y).ravel(), 0 * x.ravel(), 0 * x.ravel(), (mx, my, mz), 1.0)
+    for cells in (False, True):
+        w, q = O.vorticity_q(gs, (mx, my, mz), cells)
+        assert np.allclose(w, 0.4) and np.allclose(q, 0.0)
