@@ -19,6 +19,8 @@ stores as float32 are given float32 values on input). The script writes:
                       change and ``monitors()``.
 * ``heat_cases.npz``- one ``lbm_step`` with the D3Q7 temperature block (``Heat``)
                       over the finned ``HeatSink``, quiet and report.
+* ``wing_cases.npz``- one ``wing_step`` of the pitch-plunge NACA 0012 section
+                      (``flutter.py``) per collision model, and ``wing_init``.
 
 Nothing reads the reference at test time; only these files are used.
 """
@@ -250,6 +252,80 @@ def make_heat_cases(ref_dir):
     np.savez_compressed(os.path.join(HERE, "heat_cases.npz"), **out)
 
 
+# (name, collision, report, state h, alpha, dh/dt, dalpha/dt): one wing_step of
+# the pitch-plunge NACA 0012 section (flutter.py:20-130)
+WING_CASES = [("wing_les_report", "les", True, (0.7, 0.12, 0.003, 0.0015)),
+              ("wing_trt_quiet", "trt", False, (-1.2, -0.2, -0.002, 0.001)),
+              ("wing_bgk_report", "bgk", True, (0.0, 0.05, 0.0, -0.002))]
+WNX, WNY, WNZ, WCHORD, WEA = 48, 24, 2, 16.0, 0.4
+
+
+def import_flutter(ref_dir):
+    lbm = tack_shim.import_reference(ref_dir)
+    sys.modules.pop("flutter", None)
+    import flutter  # noqa: E402  (the reference module, on the shim)
+    import math
+    flutter.sqrt, flutter.sin, flutter.cos = math.sqrt, math.sin, math.cos
+    return lbm, flutter
+
+
+def make_wing_cases(ref_dir):
+    lbm, flutter = import_flutter(ref_dir)
+    n = WNX * WNY * WNZ
+    out, meta = {}, {}
+    for k, (name, coll, report, state) in enumerate(WING_CASES):
+        rng = np.random.default_rng(500 + k)
+        lat = lbm.D3Q19(WNX, WNY, WNZ)
+        nu = 0.01 + 0.004 * k
+        phys = lbm.COLLISIONS[coll](nu)
+        st = tack_shim.HostManagedArray(4)
+        st.numpy[:] = state
+        load = tack_shim.HostManagedArray(3)
+        geo = flutter.Wing(WCHORD, 0.25 * WNX, 0.5 * WNY, WEA, st.tack, load.tack)
+        u0, s0, strength = 0.06, 36.0, 0.9
+        flow = lbm.Flow(u0, s0, strength)
+        idx = np.arange(n)
+        x, y, z = idx % WNX, (idx // WNX) % WNY, idx // (WNX * WNY)
+        solid = np.array([geo.solid(int(a), int(b), int(c)) for a, b, c in zip(x, y, z)])
+        cvec = np.array([lbm.CX, lbm.CY, lbm.CZ]).T
+        w = np.array(lbm.W, np.float32).astype(np.float64)
+        rho = 1 + 0.01 * rng.standard_normal(n)
+        u = np.array([u0, 0.0, 0.0]) + 0.02 * rng.standard_normal((n, 3))
+        cu = 3.0 * (u @ cvec.T)
+        f = w * rho[:, None] * (1 + cu + 0.5 * cu ** 2 - 1.5 * (u ** 2).sum(1)[:, None])
+        f += 1e-3 * rng.standard_normal((n, 19))
+        f_in = np.ascontiguousarray(f.T.reshape(-1)).astype(np.float32)
+        fields = {key: tack_shim.HostManagedArray(n) for key in lbm.FIELDS}
+        diag = (lbm.Report if report else lbm.Quiet)({k_: v.tack for k_, v in fields.items()})
+        a_in = lbm.tack.array(f_in)
+        a_out = lbm.tack.empty((19 * n,))
+        t0 = time.perf_counter()
+        flutter.wing_step(lat, phys, geo, flow, diag, a_in, a_out)
+        print(f"{name}: {time.perf_counter() - t0:.2f} s, solid {int(solid.sum())}, load {load.numpy}")
+        out[f"{name}/f_in"] = f_in
+        out[f"{name}/f_out"] = np.asarray(a_out)
+        out[f"{name}/solid"] = solid.astype(np.uint8)
+        out[f"{name}/load"] = np.asarray(load.numpy)
+        if report:
+            for key in ("ux", "uy", "uz", "p", "vmag"):
+                out[f"{name}/fields/{key}"] = np.asarray(fields[key].numpy)
+        meta[name] = dict(nx=WNX, ny=WNY, nz=WNZ, collision=coll, nu=nu, report=report, u0=u0,
+                          sponge_start=s0, sponge_strength=strength, chord=WCHORD, x_ea=0.25 * WNX,
+                          y_ea=0.5 * WNY, ea=WEA, state=list(state))
+    # wing_init at a displaced state
+    lat = lbm.D3Q19(WNX, WNY, WNZ)
+    st = tack_shim.HostManagedArray(4)
+    st.numpy[:] = (0.5, -0.1, 0.0, 0.0)
+    geo = flutter.Wing(WCHORD, 0.25 * WNX, 0.5 * WNY, WEA, st.tack, tack_shim.HostManagedArray(3).tack)
+    f0 = lbm.tack.empty((19 * n,))
+    flutter.wing_init(lat, geo, lbm.Flow(0.06, 36.0, 0.9), f0)
+    out["init/f"] = np.asarray(f0)
+    meta["init"] = dict(nx=WNX, ny=WNY, nz=WNZ, u0=0.06, chord=WCHORD, x_ea=0.25 * WNX, y_ea=0.5 * WNY,
+                        ea=WEA, state=[0.5, -0.1, 0.0, 0.0])
+    out["meta"] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(HERE, "wing_cases.npz"), **out)
+
+
 def make_solver_cases(ref_dir):
     lbm = tack_shim.import_reference(ref_dir)
     out, meta = {}, {}
@@ -287,6 +363,7 @@ def main():
     make_init_cases(ref_dir)
     make_solver_cases(ref_dir)
     make_heat_cases(ref_dir)
+    make_wing_cases(ref_dir)
 
 
 if __name__ == "__main__":

@@ -59,3 +59,27 @@ def heat_cases():
             case["q_solid"] = z[f"{name}/q_solid"]
             case["fields"] = {k: z[f"{name}/fields/{k}"] for k in O.FIELDS}
         yield case
+
+
+def wing_cases():
+    from oracle import flutter_oracle as FO
+    z, meta = load("wing_cases")
+    for name, m in meta.items():
+        if name == "init":
+            continue
+        keys = ("collision", "nu", "u0", "sponge_start", "sponge_strength", "chord", "x_ea", "y_ea", "ea")
+        cfg = FO.WingConfig(m["nx"], m["ny"], m["nz"], state=tuple(m["state"]), **{k: m[k] for k in keys})
+        case = {"name": name, "cfg": cfg, "report": m["report"], "f_in": z[f"{name}/f_in"],
+                "f_out": z[f"{name}/f_out"], "solid": z[f"{name}/solid"], "load": z[f"{name}/load"]}
+        if m["report"]:
+            case["fields"] = {k: z[f"{name}/fields/{k}"] for k in ("ux", "uy", "uz", "p", "vmag")}
+        yield case
+
+
+def wing_init_case():
+    from oracle import flutter_oracle as FO
+    z, meta = load("wing_cases")
+    m = meta["init"]
+    cfg = FO.WingConfig(m["nx"], m["ny"], m["nz"], m["chord"], m["x_ea"], m["y_ea"], m["ea"],
+                        state=tuple(m["state"]), u0=m["u0"])
+    return cfg, z["init/f"]

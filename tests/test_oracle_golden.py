@@ -157,3 +157,25 @@ def test_velocity_gradient_of_a_linear_field():
     for cells in (False, True):
         w, q = O.vorticity_q(gs, (mx, my, mz), cells)
         assert np.allclose(w, 0.4) and np.allclose(q, 0.0)
+
+
+@pytest.mark.parametrize("case", list(goldens.wing_cases()), ids=lambda c: c["name"])
+def test_wing_step_golden(case):
+    """The pitch-plunge wing step (flutter.py:61-130) against the reference kernel."""
+    from oracle import flutter_oracle as FO
+    cfg = case["cfg"]
+    idx = np.arange(cfg.n)
+    assert np.array_equal(FO.solid(cfg, idx % cfg.nx, (idx // cfg.nx) % cfg.ny).astype(np.uint8), case["solid"])
+    fields = {k: np.zeros(cfg.n) for k in ("ux", "uy", "uz", "p", "vmag")}
+    f, load = FO.step(cfg, case["f_in"], fields, report=case["report"])
+    assert np.abs(f.reshape(-1) - case["f_out"]).max() < 1e-12
+    assert np.allclose(load, case["load"], rtol=1e-12, atol=1e-12)
+    if case["report"]:
+        for k, v in case["fields"].items():
+            assert np.abs(fields[k] - v).max() < 1e-12, k
+
+
+def test_wing_init_golden():
+    from oracle import flutter_oracle as FO
+    cfg, f = goldens.wing_init_case()
+    assert np.abs(FO.init(cfg) - f).max() < 1e-15
