@@ -312,6 +312,46 @@ lbm_status lbm_heat_field(lbm_solver *s, int32_t id, float **ptr);
 lbm_status lbm_set_heat_populations(lbm_solver *s, const void *g, int32_t dtype, int32_t where);
 lbm_status lbm_get_heat_populations(lbm_solver *s, void *g, int32_t dtype, int32_t where);
 
+/* ---------------------------------------------------------------------------
+ * Pitch-plunge wing (tack-lbm flutter.py:20-130): a rigid NACA 0012 section
+ * spanning z on a lattice periodic in x, y and z, moving with the plunge h
+ * and pitch alpha about its elastic axis (x_ea, y_ea) at chord fraction ea.
+ * The structure is integrated by the caller; every step takes the state
+ * {h, alpha, dh/dt, dalpha/dt} and returns the momentum-exchange force and its
+ * moment about the displaced elastic axis, summed over the lattice (not per
+ * unit span). FP32 populations on A/B buffers.
+ */
+typedef struct lbm_wing_config {
+    int32_t nx, ny, nz;
+    int32_t collision;           /* LBM_BGK | LBM_TRT | LBM_LES */
+    double nu, cs, magic;
+    double chord, x_ea, y_ea, ea;
+    double u0, sponge_start, sponge_strength;
+    int32_t device;
+    int32_t reserved;
+} lbm_wing_config;
+
+typedef struct lbm_wing lbm_wing;
+
+lbm_status lbm_wing_create(const lbm_wing_config *cfg, lbm_wing **out);
+lbm_status lbm_wing_destroy(lbm_wing *w);
+/* wing_init (flutter.py:51-58): equilibrium at rho = 1, u = (u0 (1 - solid), 0, 0). */
+lbm_status lbm_wing_init(lbm_wing *w, const double state[4]);
+/* wing_step (flutter.py:61-130); report != 0 writes ux, uy, uz, p, vmag.
+ * Synchronous: load = {fx, fy, mz}. */
+lbm_status lbm_wing_step(lbm_wing *w, int32_t report, const double state[4], double load[3]);
+lbm_status lbm_wing_set_physics(lbm_wing *w, int32_t collision, double nu);
+/* Managed pointer to field id (0..4: ux, uy, uz, p, vmag; n floats). */
+lbm_status lbm_wing_field(lbm_wing *w, int32_t id, float **ptr);
+/* Copy the current populations (19 n floats, f[q*n + idx]) from (set = 0) or to (set = 1) `host`. */
+lbm_status lbm_wing_populations(lbm_wing *w, float *host, int32_t set);
+/* The solid mask (n bytes) at `state`. */
+lbm_status lbm_wing_mask(lbm_wing *w, const double state[4], uint8_t *host);
+/* Output grid: the five fields subsampled by `stride` (flutter.py:207-211). */
+lbm_status lbm_wing_set_output_stride(lbm_wing *w, int32_t stride);
+lbm_status lbm_wing_output(lbm_wing *w, int32_t id, float **ptr, int64_t *count);
+lbm_status lbm_wing_update_output(lbm_wing *w);
+
 /* Message of the last error on this thread ("" when none). */
 const char *lbm_last_error(void);
 

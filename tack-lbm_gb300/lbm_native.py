@@ -70,6 +70,19 @@ class AdjConfig(ctypes.Structure):
     ]
 
 
+class WingConfig(ctypes.Structure):
+    """struct lbm_wing_config."""
+
+    _fields_ = [
+        ("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32), ("collision", ctypes.c_int32),
+        ("nu", ctypes.c_double), ("cs", ctypes.c_double), ("magic", ctypes.c_double),
+        ("chord", ctypes.c_double), ("x_ea", ctypes.c_double), ("y_ea", ctypes.c_double), ("ea", ctypes.c_double),
+        ("u0", ctypes.c_double), ("sponge_start", ctypes.c_double), ("sponge_strength", ctypes.c_double),
+        ("device", ctypes.c_int32), ("reserved", ctypes.c_int32),
+    ]
+
+
+_D4 = ctypes.POINTER(ctypes.c_double)
 _SIGNATURES = {
     "lbm_abi_version": (ctypes.c_int32, []),
     "lbm_last_error": (ctypes.c_char_p, []),
@@ -115,6 +128,18 @@ _SIGNATURES = {
                                                 ctypes.c_int32]),
     "lbm_get_heat_populations": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
                                                 ctypes.c_int32]),
+    "lbm_wing_create": (ctypes.c_int, [ctypes.POINTER(WingConfig), ctypes.POINTER(ctypes.c_void_p)]),
+    "lbm_wing_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "lbm_wing_init": (ctypes.c_int, [ctypes.c_void_p, _D4]),
+    "lbm_wing_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _D4, _D4]),
+    "lbm_wing_set_physics": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double]),
+    "lbm_wing_field": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]),
+    "lbm_wing_populations": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
+    "lbm_wing_mask": (ctypes.c_int, [ctypes.c_void_p, _D4, ctypes.c_void_p]),
+    "lbm_wing_set_output_stride": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "lbm_wing_output": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p),
+                                       ctypes.POINTER(ctypes.c_int64)]),
+    "lbm_wing_update_output": (ctypes.c_int, [ctypes.c_void_p]),
     "lbm_adj_create": (ctypes.c_int, [ctypes.POINTER(AdjConfig), ctypes.POINTER(ctypes.c_void_p)]),
     "lbm_adj_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "lbm_adj_set_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
