@@ -143,13 +143,16 @@ def dist_setup(n_gpus):
 def barrier(dist, torch):
     if dist is not None:
         dist.barrier()
-        torch.cuda.synchronize()
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
 
 
 def max_over_ranks(value, dist, torch):
+    """The largest value over the ranks (the job's time is its slowest replica's)."""
     if dist is None:
         return value
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
