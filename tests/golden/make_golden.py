@@ -21,6 +21,8 @@ stores as float32 are given float32 values on input). The script writes:
                       over the finned ``HeatSink``, quiet and report.
 * ``wing_cases.npz``- one ``wing_step`` of the pitch-plunge NACA 0012 section
                       (``flutter.py``) per collision model, and ``wing_init``.
+* ``fsi_cases.npz`` - one ``fsi_step`` of the cantilever wing (``fsi.py``: moving
+                      layers, interpolated bounce-back, per-layer loads).
 
 Nothing reads the reference at test time; only these files are used.
 """
@@ -326,6 +328,94 @@ def make_wing_cases(ref_dir):
     np.savez_compressed(os.path.join(HERE, "wing_cases.npz"), **out)
 
 
+# (name, collision, report): one fsi_step of the cantilever wing (fsi.py:25-186)
+# with a different plunge/pitch and rates in every layer
+FSI_CASES = [("fsi_les_report", "les", True), ("fsi_trt_quiet", "trt", False), ("fsi_bgk_report", "bgk", True)]
+FNX, FNY, FNZ, FCHORD, FSPAN, FEA = 36, 20, 8, 12.0, 5.5, 0.4
+
+
+def import_fsi(ref_dir):
+    """The reference fsi module on the shim. Its structural modules import MFEM at
+    module level; the kernels do not use it, so empty stand-in modules let the
+    file import (nothing of MFEM is called)."""
+    import math
+    import types
+    lbm = tack_shim.import_reference(ref_dir)
+
+    class _Stand(types.ModuleType):
+        def __getattr__(self, name):  # classes the structural modules derive from at import
+            return type(name, (), {})
+
+    mf = _Stand("mfem")
+    mf.ser = _Stand("mfem.ser")
+    sys.modules["mfem"], sys.modules["mfem.ser"] = mf, mf.ser
+    for name in ("fsi", "fsi_beam", "fsi_struct"):
+        sys.modules.pop(name, None)
+    import fsi  # noqa: E402  (the reference module, on the shim)
+    fsi.sqrt, fsi.sin, fsi.cos = math.sqrt, math.sin, math.cos
+    return lbm, fsi
+
+
+def fsi_kinematics(rng):
+    z = np.arange(FNZ) + 0.5
+    kin = np.zeros((FNZ, 4))
+    kin[:, 0] = 0.8 * (z / FSPAN) ** 2 + 0.05 * rng.standard_normal(FNZ)
+    kin[:, 1] = 0.15 * (z / FSPAN) + 0.02 * rng.standard_normal(FNZ)
+    kin[:, 2] = 0.004 * (z / FSPAN) ** 2
+    kin[:, 3] = -0.002 * (z / FSPAN)
+    return kin
+
+
+def make_fsi_cases(ref_dir):
+    lbm, fsi = import_fsi(ref_dir)
+    n = FNX * FNY * FNZ
+    out, meta = {}, {}
+    reflect = fsi._reflect_z()
+    for k, (name, coll, report) in enumerate(FSI_CASES):
+        rng = np.random.default_rng(700 + k)
+        lat = lbm.D3Q19(FNX, FNY, FNZ)
+        nu = 0.008 + 0.003 * k
+        phys = lbm.COLLISIONS[coll](nu)
+        kin_a = tack_shim.HostManagedArray(4 * FNZ)
+        kin = fsi_kinematics(rng)
+        kin_a.numpy[:] = kin.reshape(-1)
+        load = tack_shim.HostManagedArray(3 * FNZ)
+        geo = fsi.FlexWing(FCHORD, 0.25 * FNX, 0.5 * FNY, FEA, FSPAN, kin_a.tack, load.tack, reflect)
+        u0, s0, strength = 0.06, 27.0, 0.9
+        flow = lbm.Flow(u0, s0, strength)
+        cvec = np.array([lbm.CX, lbm.CY, lbm.CZ]).T
+        w = np.array(lbm.W, np.float32).astype(np.float64)
+        rho = 1 + 0.01 * rng.standard_normal(n)
+        u = np.array([u0, 0.0, 0.0]) + 0.02 * rng.standard_normal((n, 3))
+        cu = 3.0 * (u @ cvec.T)
+        f = w * rho[:, None] * (1 + cu + 0.5 * cu ** 2 - 1.5 * (u ** 2).sum(1)[:, None])
+        f += 1e-3 * rng.standard_normal((n, 19))
+        f_in = np.ascontiguousarray(f.T.reshape(-1)).astype(np.float32)
+        idx = np.arange(n)
+        x, y, z = idx % FNX, (idx // FNX) % FNY, idx // (FNX * FNY)
+        solid = np.array([geo.solid(int(a), int(b), int(c)) for a, b, c in zip(x, y, z)])
+        fields = {key: tack_shim.HostManagedArray(n) for key in lbm.FIELDS}
+        diag = (lbm.Report if report else lbm.Quiet)({k_: v.tack for k_, v in fields.items()})
+        a_in = lbm.tack.array(f_in)
+        a_out = lbm.tack.empty((19 * n,))
+        t0 = time.perf_counter()
+        fsi.fsi_step(lat, phys, geo, flow, diag, a_in, a_out)
+        print(f"{name}: {time.perf_counter() - t0:.2f} s, solid {int(solid.sum())}")
+        out[f"{name}/f_in"] = f_in
+        out[f"{name}/f_out"] = np.asarray(a_out)
+        out[f"{name}/solid"] = solid.astype(np.uint8)
+        out[f"{name}/kin"] = kin
+        out[f"{name}/load"] = np.asarray(load.numpy)
+        if report:
+            for key in ("ux", "uy", "uz", "p", "vmag"):
+                out[f"{name}/fields/{key}"] = np.asarray(fields[key].numpy)
+        meta[name] = dict(nx=FNX, ny=FNY, nz=FNZ, collision=coll, nu=nu, report=report, u0=u0,
+                          sponge_start=s0, sponge_strength=strength, chord=FCHORD, x_ea=0.25 * FNX,
+                          y_ea=0.5 * FNY, ea=FEA, span=FSPAN)
+    out["meta"] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(HERE, "fsi_cases.npz"), **out)
+
+
 def make_solver_cases(ref_dir):
     lbm = tack_shim.import_reference(ref_dir)
     out, meta = {}, {}
@@ -364,6 +454,7 @@ def main():
     make_solver_cases(ref_dir)
     make_heat_cases(ref_dir)
     make_wing_cases(ref_dir)
+    make_fsi_cases(ref_dir)
 
 
 if __name__ == "__main__":

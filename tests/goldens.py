@@ -83,3 +83,16 @@ def wing_init_case():
     cfg = FO.WingConfig(m["nx"], m["ny"], m["nz"], m["chord"], m["x_ea"], m["y_ea"], m["ea"],
                         state=tuple(m["state"]), u0=m["u0"])
     return cfg, z["init/f"]
+
+
+def fsi_cases():
+    from oracle import fsi_oracle as FS
+    z, meta = load("fsi_cases")
+    for name, m in meta.items():
+        keys = ("collision", "nu", "u0", "sponge_start", "sponge_strength", "chord", "x_ea", "y_ea", "ea", "span")
+        cfg = FS.FsiConfig(m["nx"], m["ny"], m["nz"], kin=z[f"{name}/kin"], **{k: m[k] for k in keys})
+        case = {"name": name, "cfg": cfg, "report": m["report"], "f_in": z[f"{name}/f_in"],
+                "f_out": z[f"{name}/f_out"], "solid": z[f"{name}/solid"], "load": z[f"{name}/load"]}
+        if m["report"]:
+            case["fields"] = {k: z[f"{name}/fields/{k}"] for k in ("ux", "uy", "uz", "p", "vmag")}
+        yield case

@@ -179,3 +179,20 @@ def test_wing_init_golden():
     from oracle import flutter_oracle as FO
     cfg, f = goldens.wing_init_case()
     assert np.abs(FO.init(cfg) - f).max() < 1e-15
+
+
+@pytest.mark.parametrize("case", list(goldens.fsi_cases()), ids=lambda c: c["name"])
+def test_fsi_step_golden(case):
+    """The cantilever-wing FSI step (fsi.py:81-186) against the reference kernel."""
+    from oracle import fsi_oracle as FS
+    c = case["cfg"]
+    idx = np.arange(c.n)
+    mask = FS.solid(c, idx % c.nx, (idx // c.nx) % c.ny, idx // (c.nx * c.ny))
+    assert np.array_equal(mask.astype(np.uint8), case["solid"])
+    fields = {k: np.zeros(c.n) for k in ("ux", "uy", "uz", "p", "vmag")}
+    f, load = FS.step(c, case["f_in"], fields, report=case["report"])
+    assert np.abs(f.reshape(-1) - case["f_out"]).max() < 1e-12
+    assert np.abs(load.reshape(-1) - case["load"]).max() < 1e-11
+    if case["report"]:
+        for k, v in case["fields"].items():
+            assert np.abs(fields[k] - v).max() < 1e-12, k
