@@ -352,6 +352,41 @@ lbm_status lbm_wing_set_output_stride(lbm_wing *w, int32_t stride);
 lbm_status lbm_wing_output(lbm_wing *w, int32_t id, float **ptr, int64_t *count);
 lbm_status lbm_wing_update_output(lbm_wing *w);
 
+/* ---------------------------------------------------------------------------
+ * Cantilever-wing FSI (tack-lbm fsi.py:25-186): an elastic NACA 0012 wing from
+ * a mirror root plane below z = 0 to z = span; inflow at x = 0, outflow at
+ * x = nx - 1, periodic y, mirror plane above z = nz - 1. Every step takes the
+ * kinematics of each layer z, kin[4 z .. 4 z + 3] = {h, alpha, dh/dt, dalpha/dt},
+ * and returns each layer's momentum-exchange force and moment,
+ * load[3 z .. 3 z + 2] = {fx, fy, mz} (relative to the fluid at rest).
+ * Wetted links use the interpolated (Bouzidi) bounce-back. FP32 populations.
+ */
+typedef struct lbm_fsi_config {
+    int32_t nx, ny, nz;
+    int32_t collision;           /* LBM_BGK | LBM_TRT | LBM_LES */
+    double nu, cs, magic;
+    double chord, x_ea, y_ea, ea, span;
+    double u0, sponge_start, sponge_strength;
+    int32_t device;
+    int32_t reserved;
+} lbm_fsi_config;
+
+typedef struct lbm_fsi lbm_fsi;
+
+lbm_status lbm_fsi_create(const lbm_fsi_config *cfg, lbm_fsi **out);
+lbm_status lbm_fsi_destroy(lbm_fsi *w);
+/* fsi_init (fsi.py:71-78) at the layer kinematics kin (4 nz values). */
+lbm_status lbm_fsi_init(lbm_fsi *w, const double *kin);
+/* fsi_step (fsi.py:81-186). Synchronous: load receives 3 nz values. */
+lbm_status lbm_fsi_step(lbm_fsi *w, int32_t report, const double *kin, double *load);
+lbm_status lbm_fsi_set_physics(lbm_fsi *w, int32_t collision, double nu);
+lbm_status lbm_fsi_field(lbm_fsi *w, int32_t id, float **ptr);
+lbm_status lbm_fsi_populations(lbm_fsi *w, float *host, int32_t set);
+lbm_status lbm_fsi_mask(lbm_fsi *w, const double *kin, uint8_t *host);
+lbm_status lbm_fsi_set_output_stride(lbm_fsi *w, int32_t stride);
+lbm_status lbm_fsi_output(lbm_fsi *w, int32_t id, float **ptr, int64_t *count);
+lbm_status lbm_fsi_update_output(lbm_fsi *w);
+
 /* Message of the last error on this thread ("" when none). */
 const char *lbm_last_error(void);
 

@@ -23,7 +23,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblbm_gb300.so")
 UNITS = ["lbm_api.cu", "lbm_kernels_f32.cu", "lbm_kernels_f16.cu", "lbm_kernels_bf16.cu",
          "lbm_kernels_f64.cu", "lbm_static_sums.cu", "lbm_adjoint.cu",
-         "lbm_heat.cu", "lbm_derived.cu", "lbm_wing.cu"]
+         "lbm_heat.cu", "lbm_derived.cu", "lbm_wing.cu", "lbm_fsi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "-diag-suppress", "128", "-I", os.path.join(ROOT, "include")]

@@ -1,0 +1,489 @@
+// lbm_fsi.cu - the cantilever-wing FSI step (tack-lbm fsi.py:25-186) and its C ABI.
+//
+// An elastic NACA 0012 wing from the root plane (a mirror below z = 0) to
+// z = span: every lattice layer z has its own plunge h, pitch alpha and their
+// rates, given by the caller's structural model each step. Per step:
+//   * fsi_mask_kernel evaluates each cell's layer section test in float64
+//     into a byte mask (fsi.py:35-47);
+//   * fsi_step_kernel (float32 populations on A/B buffers f[q*n + idx]):
+//     inflow at x = 0 from the free-stream equilibrium, zero-gradient outflow
+//     at x = nx - 1, periodic y, mirror planes below z = 0 and above
+//     z = nz - 1; moving-wall bounce-back, second order on wetted links by the
+//     interpolated (Bouzidi) rule with the wall's place on the link found by
+//     six bisection steps of the float64 section test (fsi.py:49-60,
+//     110-126); the momentum exchange relative to the fluid at rest (fsi.py:
+//     128-135), reduced per block (all of a block's cells share a layer) and
+//     added to the layer's float64 totals; the collision; the sponge, which
+//     settles density and the non-equilibrium part while solid cells take the
+//     wall velocity (fsi.py:158-172); report fields ux, uy, uz, p, vmag.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "lbm_device.cuh"
+#include "lbm_host.h"
+
+namespace lbmf {
+
+using namespace lbmk;
+
+// per layer: h, alpha, dh/dt, dalpha/dt, cos alpha, sin alpha
+constexpr int KIN = 6;
+
+struct FsiArgs {
+  const float *fin;
+  float *fout;
+  const uint8_t *mask;
+  const double *kin;
+  double *load;  // 3 per layer
+  float *fld[5];
+  int nx, ny, nz, n;
+  double chord, x_ea, y_ea, ea, span;
+  float u0, sponge_start, inv_sponge_len, sponge_strength;
+  float omega_bgk, tau0, smag_c, magic;
+};
+
+__device__ __forceinline__ bool section(const FsiArgs &a, double x, double y, int z) {
+  const double *k = a.kin + KIN * z;
+  const double dx = x - a.x_ea, dy = y - (a.y_ea + k[0]);
+  const double s = dx * k[4] - dy * k[5], t = dx * k[5] + dy * k[4];
+  const double xc = s / a.chord + a.ea;
+  const double c = fmin(fmax(xc, 0.0), 1.0);
+  const double half = 0.6 * a.chord * (0.2969 * sqrt(c) - 0.1260 * c - 0.3516 * c * c + 0.2843 * c * c * c -
+                                       0.1036 * c * c * c * c);
+  return xc >= 0.0 && xc <= 1.0 && fabs(t) < half && (double)z + 0.5 < a.span;
+}
+
+__global__ void fsi_mask_kernel(const __grid_constant__ FsiArgs a, uint8_t *mask) {
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < a.n; idx += gridDim.x * blockDim.x) {
+    const int x = idx % a.nx, y = (idx / a.nx) % a.ny, z = idx / (a.nx * a.ny);
+    mask[idx] = section(a, (double)x, (double)y, z) ? 1 : 0;
+  }
+}
+
+// the wall's place on the link from (x, y, z) toward (x - cx, y - cy, zs), as a fraction
+__device__ __forceinline__ double wall_fraction(const FsiArgs &a, int x, int y, int z, int cxq, int cyq, int zs) {
+  double lo = 0.0, hi = 1.0;
+  for (int it = 0; it < 6; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    const bool in = section(a, (double)x - mid * cxq, (double)y - mid * cyq, mid >= 0.5 ? zs : z);
+    if (in) hi = mid;
+    else lo = mid;
+  }
+  return 0.5 * (lo + hi);
+}
+
+template <int COLL, bool REPORT>
+__global__ void __launch_bounds__(BX * BY) fsi_step_kernel(const __grid_constant__ FsiArgs a) {
+  const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
+  float fx = 0.f, fy = 0.f, mz = 0.f;
+  if (x < a.nx && y < a.ny) {
+    const int idx = (z * a.ny + y) * a.nx + x;
+    const bool here = a.mask[idx] != 0;
+    const float hz = (float)a.kin[KIN * z];
+    float d[Q];
+    static_for<Q>([&](auto qc) {
+      constexpr int q = decltype(qc)::value;
+      constexpr int o = opp(q);
+      const int xr = x - cx(q);
+      const int xs = xr < 0 ? 0 : (xr > a.nx - 1 ? a.nx - 1 : xr);
+      int ys = y - cy(q);
+      ys += ys < 0 ? a.ny : 0;
+      ys -= ys >= a.ny ? a.ny : 0;
+      const int zr = z - cz(q);
+      const bool flip = zr < 0 || zr > a.nz - 1;
+      const int zs = zr < 0 ? 0 : (zr > a.nz - 1 ? a.nz - 1 : zr);
+      constexpr int mq = dir(cx(q), cy(q), -cz(q));
+      const int src = (zs * a.ny + ys) * a.nx + xs;
+      float pulled;
+      if (xr < 0) {
+        pulled = wq(q) * (1.f + 3.f * (float)cx(q) * a.u0 + 4.5f * (float)(cx(q) * cx(q)) * a.u0 * a.u0 -
+                          1.5f * a.u0 * a.u0);
+      } else {
+        pulled = a.fin[(size_t)(flip ? mq : q) * a.n + src];
+      }
+      float val = pulled;
+      if (a.mask[src]) {
+        const float bounced = a.fin[(size_t)o * a.n + idx];
+        const double *k = a.kin + KIN * zs;
+        const float kh = (float)k[0], kdh = (float)k[2], kda = (float)k[3];
+        float px = (float)x - 0.5f * (float)cx(q), py = (float)y - 0.5f * (float)cy(q);
+        float cu = (float)cx(q) * (kda * (py - (float)a.y_ea - kh)) + (float)cy(q) * (kdh - kda * (px - (float)a.x_ea));
+        float back = bounced + 6.f * wq(q) * cu;
+        if (!here) {
+          const double delta = wall_fraction(a, x, y, z, cx(q), cy(q), zs);
+          const float df = (float)delta;
+          px = (float)x - df * (float)cx(q);
+          py = (float)y - df * (float)cy(q);
+          cu = (float)cx(q) * (kda * (py - (float)a.y_ea - kh)) + (float)cy(q) * (kdh - kda * (px - (float)a.x_ea));
+          if (delta >= 0.5) {
+            back = (bounced + (2.f * df - 1.f) * a.fin[(size_t)q * a.n + idx] + 6.f * wq(q) * cu) / (2.f * df);
+          } else {
+            int xn = x + cx(q);
+            xn += xn < 0 ? a.nx : 0;
+            xn -= xn >= a.nx ? a.nx : 0;
+            int yn = y + cy(q);
+            yn += yn < 0 ? a.ny : 0;
+            yn -= yn >= a.ny ? a.ny : 0;
+            const int zn = z + cz(q);
+            const int zc = zn < 0 ? 0 : (zn > a.nz - 1 ? a.nz - 1 : zn);
+            const int nidx = (zc * a.ny + yn) * a.nx + xn;
+            if (zn == zc && !a.mask[nidx]) {
+              const float behind = a.fin[(size_t)o * a.n + nidx];
+              back = 2.f * df * bounced + (1.f - 2.f * df) * behind + 6.f * wq(q) * cu;
+            }
+          }
+          // momentum exchange relative to the fluid at rest
+          const float hit = bounced + back - 2.f * wq(q);
+          const float dfx = hit * (float)(-cx(q)), dfy = hit * (float)(-cy(q));
+          fx += dfx;
+          fy += dfy;
+          mz += (px - (float)a.x_ea) * dfy - (py - (float)a.y_ea - hz) * dfx;
+        }
+        val = back;
+      }
+      d[q] = val;
+    });
+    Pairs<float> pr;
+    const Moments<float> mo = moments<float, false>(d, !here, pr);
+    float post[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) post[q] = d[q];
+    collide<float, COLL, false>(post, mo, pr, a.omega_bgk, a.tau0, a.smag_c, a.magic);
+    const float t = fmaxf(0.f, ((float)x - a.sponge_start) * a.inv_sponge_len);
+    const float sigma = here ? 1.f : a.sponge_strength * t * t;
+    const double *k = a.kin + KIN * z;
+    const float wx = (float)k[3] * ((float)y - (float)a.y_ea - (float)k[0]);
+    const float wy = (float)k[2] - (float)k[3] * ((float)x - (float)a.x_ea);
+    const float rho_s = mo.rho + sigma * (1.f - mo.rho);
+    const float usx = here ? wx : mo.ux, usy = here ? wy : mo.uy, usz = here ? 0.f : mo.uz;
+    float e0[Q], e1[Q];
+    feq_val<float, false>(mo.rho, mo.rho, mo.ux, mo.uy, mo.uz, e0);
+    feq_val<float, false>(rho_s, rho_s, usx, usy, usz, e1);
+    const float keep = 1.f - sigma;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) a.fout[(size_t)q * a.n + idx] = e1[q] + keep * (post[q] - e0[q]);
+    if (REPORT) {
+      a.fld[0][idx] = mo.ux;
+      a.fld[1][idx] = mo.uy;
+      a.fld[2][idx] = mo.uz;
+      a.fld[3][idx] = mo.drho * (1.f / 3.f);
+      a.fld[4][idx] = sqrtf(mo.ux * mo.ux + mo.uy * mo.uy + mo.uz * mo.uz);
+    }
+  }
+  __shared__ float red[BY][3];
+  float v[3] = {fx, fy, mz};
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[c] += __shfl_down_sync(0xffffffffu, v[c], o);
+  }
+  if (threadIdx.x == 0)
+    for (int c = 0; c < 3; ++c) red[threadIdx.y][c] = v[c];
+  __syncthreads();
+  if (threadIdx.y == 0 && threadIdx.x < 3) {
+    float s = 0.f;
+    for (int w = 0; w < BY; ++w) s += red[w][threadIdx.x];
+    if (s != 0.f) atomicAdd(&a.load[3 * z + threadIdx.x], (double)s);
+  }
+}
+
+__global__ void fsi_init_kernel(float *f, const uint8_t *mask, int n, float u0) {
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    float eq[Q];
+    feq_val<float, false>(1.f, 1.f, mask[idx] ? 0.f : u0, 0.f, 0.f, eq);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) f[(size_t)q * n + idx] = eq[q];
+  }
+}
+
+__global__ void fsi_coarsen_kernel(const float *const *src, float *const *dst, int nx, int ny, int s, int mx, int my,
+                                   int m) {
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < m; idx += gridDim.x * blockDim.x) {
+    const int i = idx % mx, j = (idx / mx) % my, k = idx / (mx * my);
+    const int from = ((k * s) * ny + j * s) * nx + i * s;
+#pragma unroll
+    for (int c = 0; c < 5; ++c) dst[c][idx] = src[c][from];
+  }
+}
+
+}  // namespace lbmf
+
+struct lbm_fsi {
+  lbm_fsi_config cfg;
+  int64_t n;
+  float *f[2] = {nullptr, nullptr};
+  int cur = 0;
+  uint8_t *mask = nullptr;
+  double *kin = nullptr;
+  double *load = nullptr;
+  float *fld[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  int stride = 1;
+  int out_dims[3] = {0, 0, 0};
+  float *out[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  float **ptrs = nullptr;
+};
+
+namespace {
+
+lbm_status ffail(lbm_status s, const std::string &msg) {
+  lbmh::set_last_error(msg);
+  return s;
+}
+
+#define FCUDA(call)                                                                              \
+  do {                                                                                           \
+    cudaError_t e_ = (call);                                                                     \
+    if (e_ != cudaSuccess) return ffail(LBM_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+lbm_status fvalidate(const lbm_fsi_config &c) {
+  if (c.nx < 2 || c.ny < 2 || c.nz < 1 || (int64_t)c.nx * c.ny * c.nz > (int64_t)INT32_MAX / 19)
+    return ffail(LBM_ERR_ARG, "lattice sizes out of range");
+  if ((c.ny + lbmk::BY - 1) / lbmk::BY > 65535 || c.nz > 65535) return ffail(LBM_ERR_ARG, "ny/4 and nz must be <= 65535");
+  if (c.collision < LBM_BGK || c.collision > LBM_LES) return ffail(LBM_ERR_ARG, "unknown collision model");
+  if (!(std::isfinite(c.nu) && c.nu > 0.0)) return ffail(LBM_ERR_ARG, "nu must be finite and > 0");
+  if (!(c.chord > 0.0) || !std::isfinite(c.chord)) return ffail(LBM_ERR_ARG, "chord must be > 0");
+  const double v[] = {c.cs, c.magic, c.x_ea, c.y_ea, c.ea, c.span, c.u0, c.sponge_start, c.sponge_strength};
+  for (double x : v)
+    if (!std::isfinite(x)) return ffail(LBM_ERR_ARG, "configuration values must be finite");
+  if (!(c.sponge_start < c.nx)) return ffail(LBM_ERR_ARG, "sponge_start must be < nx");
+  return LBM_OK;
+}
+
+void frelease(lbm_fsi *w) {
+  cudaFree(w->f[0]);
+  cudaFree(w->f[1]);
+  cudaFree(w->mask);
+  cudaFree(w->kin);
+  cudaFree(w->load);
+  for (int k = 0; k < 5; ++k) {
+    if (w->stride > 1) cudaFree(w->out[k]);
+    cudaFree(w->fld[k]);
+  }
+  cudaFree(w->ptrs);
+}
+
+lbmf::FsiArgs fargs(const lbm_fsi *w) {
+  const lbm_fsi_config &c = w->cfg;
+  lbmf::FsiArgs a{};
+  a.mask = w->mask;
+  a.kin = w->kin;
+  a.load = w->load;
+  for (int k = 0; k < 5; ++k) a.fld[k] = w->fld[k];
+  a.nx = c.nx;
+  a.ny = c.ny;
+  a.nz = c.nz;
+  a.n = (int)w->n;
+  a.chord = c.chord;
+  a.x_ea = c.x_ea;
+  a.y_ea = c.y_ea;
+  a.ea = c.ea;
+  a.span = c.span;
+  a.u0 = (float)c.u0;
+  a.sponge_start = (float)c.sponge_start;
+  a.inv_sponge_len = (float)(1.0 / ((double)c.nx - c.sponge_start));
+  a.sponge_strength = (float)c.sponge_strength;
+  a.omega_bgk = (float)(1.0 / (3.0 * c.nu + 0.5));
+  a.tau0 = (float)(3.0 * c.nu + 0.5);
+  a.smag_c = (float)(25.456 * c.cs * c.cs);
+  a.magic = (float)c.magic;
+  return a;
+}
+
+// upload the layer kinematics (with cos, sin of each pitch) and build the mask
+lbm_status set_kin(lbm_fsi *w, const double *kin) {
+  std::vector<double> k((size_t)lbmf::KIN * w->cfg.nz);
+  for (int z = 0; z < w->cfg.nz; ++z) {
+    for (int j = 0; j < 4; ++j) k[lbmf::KIN * z + j] = kin[4 * z + j];
+    k[lbmf::KIN * z + 4] = std::cos(kin[4 * z + 1]);
+    k[lbmf::KIN * z + 5] = std::sin(kin[4 * z + 1]);
+  }
+  FCUDA(cudaMemcpy(w->kin, k.data(), k.size() * sizeof(double), cudaMemcpyHostToDevice));
+  lbmf::fsi_mask_kernel<<<lbmk::cell_grid(w->n), 256>>>(fargs(w), w->mask);
+  FCUDA(cudaGetLastError());
+  return LBM_OK;
+}
+
+template <int COLL>
+void launch_fsi(const lbm_fsi *w, const lbmf::FsiArgs &a, bool report) {
+  const dim3 block(lbmk::BX, lbmk::BY);
+  const dim3 grid((w->cfg.nx + lbmk::BX - 1) / lbmk::BX, (w->cfg.ny + lbmk::BY - 1) / lbmk::BY, w->cfg.nz);
+  if (report) lbmf::fsi_step_kernel<COLL, true><<<grid, block>>>(a);
+  else lbmf::fsi_step_kernel<COLL, false><<<grid, block>>>(a);
+}
+
+lbm_status fset_ptrs(lbm_fsi *w) {
+  float *h[10];
+  for (int k = 0; k < 5; ++k) {
+    h[k] = w->fld[k];
+    h[5 + k] = w->out[k];
+  }
+  FCUDA(cudaMemcpy(w->ptrs, h, sizeof(h), cudaMemcpyHostToDevice));
+  return LBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+lbm_status lbm_fsi_create(const lbm_fsi_config *cfg, lbm_fsi **out) {
+  if (!cfg || !out) return ffail(LBM_ERR_ARG, "null argument");
+  *out = nullptr;
+  lbm_status st = fvalidate(*cfg);
+  if (st != LBM_OK) return st;
+  FCUDA(cudaSetDevice(cfg->device));
+  lbm_fsi *w = new (std::nothrow) lbm_fsi();
+  if (!w) return ffail(LBM_ERR_ARG, "out of host memory");
+  w->cfg = *cfg;
+  w->n = (int64_t)cfg->nx * cfg->ny * cfg->nz;
+  w->out_dims[0] = cfg->nx;
+  w->out_dims[1] = cfg->ny;
+  w->out_dims[2] = cfg->nz;
+  const size_t fb = (size_t)19 * w->n * sizeof(float);
+  cudaError_t e = cudaMalloc(&w->f[0], fb);
+  if (e == cudaSuccess) e = cudaMalloc(&w->f[1], fb);
+  if (e == cudaSuccess) e = cudaMalloc(&w->mask, (size_t)w->n);
+  if (e == cudaSuccess) e = cudaMalloc(&w->kin, (size_t)lbmf::KIN * cfg->nz * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemset(w->kin, 0, (size_t)lbmf::KIN * cfg->nz * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&w->load, (size_t)3 * cfg->nz * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&w->ptrs, 10 * sizeof(float *));
+  for (int k = 0; k < 5 && e == cudaSuccess; ++k) {
+    e = cudaMallocManaged(&w->fld[k], (size_t)w->n * sizeof(float), cudaMemAttachGlobal);
+    if (e == cudaSuccess) e = cudaMemset(w->fld[k], 0, (size_t)w->n * sizeof(float));
+    w->out[k] = w->fld[k];
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    frelease(w);
+    delete w;
+    return ffail(LBM_ERR_CUDA, std::string("lbm_fsi_create: ") + cudaGetErrorString(e));
+  }
+  *out = w;
+  return LBM_OK;
+}
+
+lbm_status lbm_fsi_destroy(lbm_fsi *w) {
+  if (!w) return LBM_OK;
+  cudaSetDevice(w->cfg.device);
+  cudaDeviceSynchronize();
+  frelease(w);
+  delete w;
+  return LBM_OK;
+}
+
+lbm_status lbm_fsi_init(lbm_fsi *w, const double *kin) {
+  if (!w || !kin) return ffail(LBM_ERR_ARG, "null argument");
+  FCUDA(cudaSetDevice(w->cfg.device));
+  lbm_status st = set_kin(w, kin);
+  if (st != LBM_OK) return st;
+  w->cur = 0;
+  lbmf::fsi_init_kernel<<<lbmk::cell_grid(w->n), 256>>>(w->f[0], w->mask, (int)w->n, (float)w->cfg.u0);
+  FCUDA(cudaGetLastError());
+  return LBM_OK;
+}
+
+lbm_status lbm_fsi_step(lbm_fsi *w, int32_t report, const double *kin, double *load) {
+  if (!w || !kin || !load) return ffail(LBM_ERR_ARG, "null argument");
+  FCUDA(cudaSetDevice(w->cfg.device));
+  lbm_status st = set_kin(w, kin);
+  if (st != LBM_OK) return st;
+  lbmf::FsiArgs a = fargs(w);
+  a.fin = w->f[w->cur];
+  a.fout = w->f[1 - w->cur];
+  FCUDA(cudaMemsetAsync(w->load, 0, (size_t)3 * w->cfg.nz * sizeof(double)));
+  switch (w->cfg.collision) {
+    case LBM_BGK: launch_fsi<lbmk::COLL_BGK>(w, a, report != 0); break;
+    case LBM_TRT: launch_fsi<lbmk::COLL_TRT>(w, a, report != 0); break;
+    default: launch_fsi<lbmk::COLL_LES>(w, a, report != 0); break;
+  }
+  FCUDA(cudaGetLastError());
+  FCUDA(cudaMemcpy(load, w->load, (size_t)3 * w->cfg.nz * sizeof(double), cudaMemcpyDeviceToHost));
+  w->cur ^= 1;
+  return LBM_OK;
+}
+
+lbm_status lbm_fsi_set_physics(lbm_fsi *w, int32_t collision, double nu) {
+  if (!w) return ffail(LBM_ERR_ARG, "null argument");
+  lbm_fsi_config c = w->cfg;
+  c.collision = collision;
+  c.nu = nu;
+  lbm_status st = fvalidate(c);
+  if (st != LBM_OK) return st;
+  w->cfg = c;
+  return LBM_OK;
+}
+
+lbm_status lbm_fsi_field(lbm_fsi *w, int32_t id, float **ptr) {
+  if (!w || !ptr) return ffail(LBM_ERR_ARG, "null argument");
+  if (id < 0 || id >= 5) return ffail(LBM_ERR_ARG, "field id out of range (ux, uy, uz, p, vmag)");
+  *ptr = w->fld[id];
+  return LBM_OK;
+}
+
+lbm_status lbm_fsi_populations(lbm_fsi *w, float *host, int32_t set) {
+  if (!w || !host) return ffail(LBM_ERR_ARG, "null argument");
+  FCUDA(cudaSetDevice(w->cfg.device));
+  const size_t fb = (size_t)19 * w->n * sizeof(float);
+  if (set) FCUDA(cudaMemcpy(w->f[w->cur], host, fb, cudaMemcpyHostToDevice));
+  else FCUDA(cudaMemcpy(host, w->f[w->cur], fb, cudaMemcpyDeviceToHost));
+  return LBM_OK;
+}
+
+lbm_status lbm_fsi_mask(lbm_fsi *w, const double *kin, uint8_t *host) {
+  if (!w || !kin || !host) return ffail(LBM_ERR_ARG, "null argument");
+  FCUDA(cudaSetDevice(w->cfg.device));
+  lbm_status st = set_kin(w, kin);
+  if (st != LBM_OK) return st;
+  FCUDA(cudaMemcpy(host, w->mask, (size_t)w->n, cudaMemcpyDeviceToHost));
+  return LBM_OK;
+}
+
+lbm_status lbm_fsi_set_output_stride(lbm_fsi *w, int32_t stride) {
+  if (!w) return ffail(LBM_ERR_ARG, "null argument");
+  if (stride < 1) return ffail(LBM_ERR_ARG, "stride must be >= 1");
+  FCUDA(cudaSetDevice(w->cfg.device));
+  FCUDA(cudaDeviceSynchronize());
+  if (w->stride > 1)
+    for (int k = 0; k < 5; ++k) cudaFree(w->out[k]);
+  const int dims[3] = {w->cfg.nx, w->cfg.ny, w->cfg.nz};
+  size_t m = 1;
+  for (int k = 0; k < 3; ++k) {
+    w->out_dims[k] = (dims[k] + stride - 1) / stride;
+    m *= (size_t)w->out_dims[k];
+  }
+  w->stride = stride;
+  for (int k = 0; k < 5; ++k) {
+    if (stride == 1) {
+      w->out[k] = w->fld[k];
+      continue;
+    }
+    FCUDA(cudaMallocManaged(&w->out[k], m * sizeof(float), cudaMemAttachGlobal));
+    FCUDA(cudaMemset(w->out[k], 0, m * sizeof(float)));
+  }
+  return fset_ptrs(w);
+}
+
+lbm_status lbm_fsi_output(lbm_fsi *w, int32_t id, float **ptr, int64_t *count) {
+  if (!w || !ptr || !count) return ffail(LBM_ERR_ARG, "null argument");
+  if (id < 0 || id >= 5) return ffail(LBM_ERR_ARG, "output id out of range (ux, uy, uz, p, vmag)");
+  *ptr = w->out[id];
+  *count = (int64_t)w->out_dims[0] * w->out_dims[1] * w->out_dims[2];
+  return LBM_OK;
+}
+
+lbm_status lbm_fsi_update_output(lbm_fsi *w) {
+  if (!w) return ffail(LBM_ERR_ARG, "null argument");
+  if (w->stride <= 1) return LBM_OK;
+  FCUDA(cudaSetDevice(w->cfg.device));
+  const int m = w->out_dims[0] * w->out_dims[1] * w->out_dims[2];
+  lbmf::fsi_coarsen_kernel<<<lbmk::cell_grid(m), 256>>>(w->ptrs, w->ptrs + 5, w->cfg.nx, w->cfg.ny, w->stride,
+                                                        w->out_dims[0], w->out_dims[1], m);
+  FCUDA(cudaGetLastError());
+  return LBM_OK;
+}
+
+}  // extern "C"

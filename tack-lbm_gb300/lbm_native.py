@@ -82,6 +82,18 @@ class WingConfig(ctypes.Structure):
     ]
 
 
+class FsiConfig(ctypes.Structure):
+    """struct lbm_fsi_config."""
+
+    _fields_ = [
+        ("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32), ("collision", ctypes.c_int32),
+        ("nu", ctypes.c_double), ("cs", ctypes.c_double), ("magic", ctypes.c_double),
+        ("chord", ctypes.c_double), ("x_ea", ctypes.c_double), ("y_ea", ctypes.c_double), ("ea", ctypes.c_double),
+        ("span", ctypes.c_double), ("u0", ctypes.c_double), ("sponge_start", ctypes.c_double),
+        ("sponge_strength", ctypes.c_double), ("device", ctypes.c_int32), ("reserved", ctypes.c_int32),
+    ]
+
+
 _D4 = ctypes.POINTER(ctypes.c_double)
 _SIGNATURES = {
     "lbm_abi_version": (ctypes.c_int32, []),
@@ -140,6 +152,18 @@ _SIGNATURES = {
     "lbm_wing_output": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p),
                                        ctypes.POINTER(ctypes.c_int64)]),
     "lbm_wing_update_output": (ctypes.c_int, [ctypes.c_void_p]),
+    "lbm_fsi_create": (ctypes.c_int, [ctypes.POINTER(FsiConfig), ctypes.POINTER(ctypes.c_void_p)]),
+    "lbm_fsi_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "lbm_fsi_init": (ctypes.c_int, [ctypes.c_void_p, _D4]),
+    "lbm_fsi_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _D4, _D4]),
+    "lbm_fsi_set_physics": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double]),
+    "lbm_fsi_field": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]),
+    "lbm_fsi_populations": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
+    "lbm_fsi_mask": (ctypes.c_int, [ctypes.c_void_p, _D4, ctypes.c_void_p]),
+    "lbm_fsi_set_output_stride": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "lbm_fsi_output": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p),
+                                      ctypes.POINTER(ctypes.c_int64)]),
+    "lbm_fsi_update_output": (ctypes.c_int, [ctypes.c_void_p]),
     "lbm_adj_create": (ctypes.c_int, [ctypes.POINTER(AdjConfig), ctypes.POINTER(ctypes.c_void_p)]),
     "lbm_adj_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "lbm_adj_set_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
