@@ -37,18 +37,21 @@ def test_fsi_golden_through_kernel_entry(case):
 
 
 class TwoModes:
-    """A two-mode cantilever: bending h = (z/span)^2, torsion alpha = z/span."""
+    """A two-mode cantilever, mass normalised for a wing of modal mass ~1e4 (fluid
+    density 1): bending h = A (z/span)^2, torsion alpha = B z/span."""
+
+    A, B = 0.01, 0.002
 
     def __init__(self, span):
         self.span = span
         self.omega0 = np.array([0.004, 0.009])
         z = np.linspace(0.0, span, 9)
-        self.h = np.stack([(z / span) ** 2, 0.1 * (z / span) ** 2])
-        self.alpha = np.stack([0.0 * z, z / span])
+        self.h = self.A * np.stack([(z / span) ** 2, 0.1 * (z / span) ** 2])
+        self.alpha = self.B * np.stack([0.0 * z, z / span])
 
     def sections_at(self, z):
         s = np.clip(np.asarray(z, float) / self.span, 0.0, None) * (np.asarray(z) < self.span)
-        return np.stack([s ** 2, 0.1 * s ** 2]), np.stack([0.0 * s, s])
+        return self.A * np.stack([s ** 2, 0.1 * s ** 2]), self.B * np.stack([0.0 * s, s])
 
 
 def test_fsi_solver_against_oracle():
@@ -63,8 +66,8 @@ def test_fsi_solver_against_oracle():
     idx = np.arange(cfg.n)
     f = s.populations().astype(np.float64)
     assert O.weight_err(f, FS.init(cfg)) <= 1e-7
-    s.release(tip_twist_rate=0.004)
-    ref.v[1] += 0.004 / fem.alpha[1, -1]
+    s.release(tip_twist_rate=2e-4)
+    ref.v[1] += 2e-4 / fem.alpha[1, -1]
     mh, ma = fem.sections_at(np.arange(8) + 0.5)
     for k in range(8):
         cfg.kin = np.stack([ref.q @ mh, ref.q @ ma, ref.v @ mh, ref.v @ ma], 1)
@@ -79,6 +82,7 @@ def test_fsi_solver_against_oracle():
         assert O.weight_err(s.populations(), f) <= 6e-6, f"step {k + 1}"
         assert np.abs(s.layer_load - load).max() <= 2e-5 * max(1e-3, np.abs(load).max()), f"step {k + 1}"
     assert np.allclose(s.structure.q, ref.q, rtol=1e-3, atol=1e-12)
+    assert abs(s.tip()[1]) > 0  # the tip has twisted
     s.update_output()
     full = s.fields["ux"].numpy.reshape(8, 24, 48)
     assert np.array_equal(s.output["ux"].numpy.reshape(s.out_dims[::-1]), full[::2, ::2, ::2])
