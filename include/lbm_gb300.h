@@ -223,13 +223,15 @@ lbm_status lbm_memory(lbm_solver *s, int64_t *bytes);
 lbm_status lbm_managed_alloc(int64_t count, float **ptr);
 lbm_status lbm_managed_free(float *ptr);
 
-/* Kernel timing: when enabled, every step records CUDA events around the bulk
- * and generic step kernels on the launching stream. lbm_timing_read
- * synchronises and returns {bulk ms total, bulk launches, bulk cells per
- * launch, generic ms total, generic launches, generic cells per launch, ms
- * from the first timed step's start to the last one's end} since the last
- * enable (at most 4096 steps are timed). (No reference counterpart:
- * measurement support.) */
+/* Kernel timing: when enabled, every step records CUDA events on the launching
+ * stream around the main step kernel (step_kernel, or stream_kernel with
+ * LBM_FLAG_BULKCOPY) and after the step's remaining work (the lid rows'
+ * general_kernel joined from its side stream, the monitor sums on report
+ * steps). lbm_timing_read synchronises and returns {main kernel ms total, main
+ * kernel launches, cells per main launch, ms total of the rest, its launches,
+ * cells per general_kernel launch, ms from the first timed step's start to the
+ * last one's end} since the last enable (at most 4096 steps are timed).
+ * (No reference counterpart: measurement support.) */
 lbm_status lbm_timing(lbm_solver *s, int32_t enable);
 lbm_status lbm_timing_read(lbm_solver *s, double out[7]);
 

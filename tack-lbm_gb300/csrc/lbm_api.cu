@@ -889,8 +889,7 @@ lbm_status lbm_timing_read(lbm_solver *s, double out[7]) {
   out[1] = c.ev_used;
   out[2] = (double)c.bulk_cells;
   out[3] = gen;
-  out[4] = 0;
-  out[5] = (double)c.generic_cells;
+  out[4] = c.ev_used;
   out[5] = (double)c.generic_cells;
   return LBM_OK;
 }
