@@ -133,7 +133,10 @@ lbm_status lbm_init_random(lbm_solver *s, double rho_sigma, double u_noise, uint
  * Replaces Solver.step (lbm.py:639-647). */
 lbm_status lbm_step(lbm_solver *s, int32_t report, void *stream);
 
-/* `count` quiet steps, the last one a report step when report_last != 0. */
+/* `count` quiet steps, the last one a report step when report_last != 0. Pairs
+ * of quiet steps are launched as one CUDA graph (captured once per parity and
+ * kept until an argument of the step changes: lbm_set_physics, lbm_set_sponge,
+ * lbm_set_actuation, lbm_set_obstacle, lbm_set_sink); not while lbm_timing is on. */
 lbm_status lbm_run(lbm_solver *s, int32_t count, int32_t report_last, void *stream);
 
 /* Synchronise and return the monitors of the last report step, in

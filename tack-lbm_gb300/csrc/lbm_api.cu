@@ -282,6 +282,15 @@ void release_output(Ctx &c) {
   c.out_dims[2] = c.cfg.nz;
 }
 
+// Forget the captured step graphs (after anything their kernels took as an
+// argument has changed).
+void drop_graphs(Ctx &c) {
+  for (cudaGraphExec_t &g : c.pair_graph) {
+    if (g) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
+}
+
 void release_timing(Ctx &c) {
   if (c.ev) {
     for (int k = 0; k < 3 * c.ev_cap; ++k) cudaEventDestroy(c.ev[k]);
@@ -303,6 +312,8 @@ void release(lbm_solver *s) {
   cudaFree(c.special);
   cudaFree(c.wmasks);
   cudaFree(c.fld_dev);
+  drop_graphs(c);
+  if (c.capture) cudaStreamDestroy(c.capture);
   if (c.side) cudaStreamDestroy(c.side);
   if (c.fork) cudaEventDestroy(c.fork);
   if (c.join) cudaEventDestroy(c.join);
@@ -452,6 +463,7 @@ lbm_status lbm_create(const lbm_config *cfg, lbm_solver **out) {
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
     cudaError_t e0 = cudaStreamCreateWithPriority(&c.side, cudaStreamNonBlocking, hi);
+    if (e0 == cudaSuccess) e0 = cudaStreamCreateWithFlags(&c.capture, cudaStreamNonBlocking);
     if (e0 == cudaSuccess) e0 = cudaEventCreateWithFlags(&c.fork, cudaEventDisableTiming);
     if (e0 == cudaSuccess) e0 = cudaEventCreateWithFlags(&c.join, cudaEventDisableTiming);
     if (e0 != cudaSuccess) {
@@ -566,18 +578,65 @@ lbm_status lbm_step(lbm_solver *s, int32_t report, void *stream) {
   return LBM_OK;
 }
 
+// One step's launches on `st` (the flow step, then the temperature step) and
+// the bookkeeping that follows them.
+static cudaError_t launch_one(lbm_solver *s, bool rep, cudaStream_t st) {
+  Ctx &c = s->c;
+  cudaError_t e = dispatch_step(c, rep, st);
+  if (e == cudaSuccess && c.cfg.heat) {
+    e = lbmh::launch_heat(c, rep, st);
+    c.g_cur ^= 1;
+  }
+  c.odd_next ^= 1;
+  return e;
+}
+
+// The graph of two quiet steps starting at parity c.odd_next, captured on the
+// solver's capture stream the first time it is needed. Null when capture is
+// not possible; the caller then launches the steps one by one.
+static cudaGraphExec_t pair_graph(lbm_solver *s) {
+  Ctx &c = s->c;
+  cudaGraphExec_t &slot = c.pair_graph[c.odd_next];
+  if (slot) return slot;
+  if (cudaStreamBeginCapture(c.capture, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  const int odd = c.odd_next, g = c.g_cur;
+  cudaError_t e = launch_one(s, false, c.capture);
+  if (e == cudaSuccess) e = launch_one(s, false, c.capture);
+  c.odd_next = odd;  // two flips: the same parity and temperature buffer again
+  c.g_cur = g;
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e2 = cudaStreamEndCapture(c.capture, &graph);
+  if (e == cudaSuccess && e2 == cudaSuccess && graph) {
+    if (cudaGraphInstantiate(&slot, graph, 0) != cudaSuccess) slot = nullptr;
+  }
+  if (graph) cudaGraphDestroy(graph);
+  cudaGetLastError();
+  return slot;
+}
+
 lbm_status lbm_run(lbm_solver *s, int32_t count, int32_t report_last, void *stream) {
   LBM_HANDLE(s);
   if (count < 0) return fail(LBM_ERR_ARG, "count must be >= 0");
-  for (int32_t k = 0; k < count; ++k) {
-    const bool rep = report_last && k == count - 1;
-    LBM_CUDA(dispatch_step(s->c, rep, (cudaStream_t)stream));
-    if (s->c.cfg.heat) {
-      LBM_CUDA(lbmh::launch_heat(s->c, rep, (cudaStream_t)stream));
-      s->c.g_cur ^= 1;
+  const cudaStream_t st = (cudaStream_t)stream;
+  const int32_t quiet = report_last ? count - 1 : count;
+  int32_t k = 0;
+  // pairs of quiet steps as graph launches (not while kernels are being timed)
+  if (!s->c.ev && quiet >= 4) {
+    while (quiet - k >= 2) {
+      cudaGraphExec_t g = pair_graph(s);
+      if (!g) break;
+      LBM_CUDA(cudaGraphLaunch(g, st));
+      s->steps += 2;
+      k += 2;
     }
+  }
+  for (; k < count; ++k) {
+    const bool rep = report_last && k == count - 1;
+    LBM_CUDA(launch_one(s, rep, st));
     if (s->c.ev && s->c.ev_used < s->c.ev_cap) s->c.ev_used++;
-    s->c.odd_next ^= 1;
     s->steps += 1;
     if (rep) s->reported = true;
   }
@@ -644,6 +703,7 @@ lbm_status lbm_set_physics(lbm_solver *s, int32_t collision, double nu, double c
   lbm_status st = validate(g);
   if (st != LBM_OK) return st;
   s->c.cfg = g;
+  drop_graphs(s->c);
   return LBM_OK;
 }
 
@@ -652,12 +712,14 @@ lbm_status lbm_set_sponge(lbm_solver *s, double start, double strength) {
   if (!std::isfinite(start) || !std::isfinite(strength)) return fail(LBM_ERR_ARG, "non-finite sponge");
   s->c.cfg.sponge_start = start;
   s->c.cfg.sponge_strength = strength;
+  drop_graphs(s->c);
   return LBM_OK;
 }
 
 lbm_status lbm_set_actuation(lbm_solver *s, double omega_rot) {
   if (!s) return fail(LBM_ERR_ARG, "null solver handle");
   if (!std::isfinite(omega_rot)) return fail(LBM_ERR_ARG, "non-finite rotation");
+  if (omega_rot != s->c.omega_rot) drop_graphs(s->c);
   s->c.omega_rot = omega_rot;
   return LBM_OK;
 }
@@ -747,6 +809,7 @@ lbm_status lbm_set_obstacle(lbm_solver *s, int32_t kind, const double geo[7]) {
     return fail(LBM_ERR_CUDA, std::string("set_obstacle: ") + cudaGetErrorString(e));
   }
   s->c.cfg = g;
+  drop_graphs(s->c);
   st = set_reach(s->c);
   if (st == LBM_OK) st = classify_segments(s);
   if (st == LBM_OK) {
@@ -957,10 +1020,12 @@ lbm_status lbm_set_sink(lbm_solver *s, const double sink[8]) {
     lbm_status st = validate(g);
     if (st != LBM_OK) return st;
     for (int k = 0; k < 8; ++k) s->c.cfg.sink[k] = sink[k];
+    drop_graphs(s->c);
     return LBM_OK;
   }
   double geo[7] = {g.ox, g.oy, g.oz, g.r, g.hx, g.hy, g.hz};
   for (int k = 0; k < 8; ++k) s->c.cfg.sink[k] = sink[k];
+  drop_graphs(s->c);
   return lbm_set_obstacle(s, LBM_HEATSINK, geo);
 }
 

@@ -41,6 +41,11 @@ struct Ctx {
   int g_cur;                 // g[g_cur] holds the current temperature populations
   float4 *aux;               // (ux, uy, uz, tau) per fluid cell, written by the flow step
   float *heat_fld[LBM_NUM_HEAT_FIELDS];
+  // lbm_run: two quiet steps (odd + even, with their lid-row and heat launches)
+  // captured as one CUDA graph per starting parity, replayed while the
+  // arguments the kernels took stay the same
+  cudaStream_t capture;
+  cudaGraphExec_t pair_graph[2];
   // optional kernel timing: events around the bulk and generic launches
   cudaEvent_t *ev;           // 3 events per step in a ring (bulk start, bulk end/generic start, generic end)
   int ev_cap, ev_used;

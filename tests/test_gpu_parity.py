@@ -373,3 +373,57 @@ def test_long_rows(G, storage, tol, kernel):
             f = g
         else:
             assert O.weight_err(get(h, cfg.n), f) <= tol, f"{storage} step {k + 1}"
+
+
+@pytest.mark.parametrize("kind", ["les_slipz", "lid_box", "heatsink_heat", "bulkcopy", "f16"])
+def test_run_graphs_match_single_steps(G, kind):
+    """lbm_run launches pairs of quiet steps as CUDA graphs: the result is the
+    same, bit for bit, as the steps launched one by one (and a parameter change
+    between runs is picked up)."""
+    cfg = O.Config(64, 20, 12, collision="les", nu=0.01, obstacle="cylinder", ox=20.3, oy=9.6, r=3.4,
+                   u0=0.07, sponge_start=50.0, sponge_strength=0.9, vertical="slip", omega_rot=0.02)
+    storage, flags = "f32", 0
+    if kind == "lid_box":
+        cfg = O.Config(64, 20, 12, collision="trt", nu=0.01, obstacle="box", ox=20.5, oy=9.0, oz=6.0, hx=3.0,
+                       hy=2.5, hz=3.0, u0=0.06, sponge_start=50.0, lateral="lid", u_lid=0.05)
+    elif kind == "heatsink_heat":
+        cfg = O.Config(64, 20, 12, collision="les", nu=0.01, obstacle="heatsink", u0=0.05, sponge_start=48.0,
+                       sink=(12, 19, 1, 9, 2, 8, 2, 4), heat=True, alpha=0.01 / 0.7, heat_nu=0.01)
+    elif kind == "bulkcopy":
+        flags = N.FLAG_BULKCOPY
+    elif kind == "f16":
+        storage = "f16"
+
+    def make():
+        h = native_handle(cfg, storage, flags=flags)
+        h.call("lbm_init_random", 1e-3, 0.01, 9)
+        return h
+
+    if cfg.heat:
+        import lbm
+        s1 = lbm.Solver(64, 20, 12, collision="les", obstacle="heatsink", reynolds=40.0, u0=0.05, diameter=6.0,
+                        heat=True)
+        s2 = lbm.Solver(64, 20, 12, collision="les", obstacle="heatsink", reynolds=40.0, u0=0.05, diameter=6.0,
+                        heat=True)
+        for s in (s1, s2):
+            s.set_wall_temperature(1.0)
+        h1, h2 = s1._h, s2._h
+    else:
+        h1, h2 = make(), make()
+    h1.call("lbm_run", 21, 1, None)
+    for k in range(21):
+        h2.call("lbm_step", int(k == 20), None)
+    if kind == "les_slipz":  # a changed argument must reach the next run
+        for h in (h1, h2):
+            h.call("lbm_set_actuation", -0.03)
+        h1.call("lbm_run", 8, 0, None)
+        for _ in range(8):
+            h2.call("lbm_step", 0, None)
+    n = cfg.n
+    assert np.array_equal(get(h1, n), get(h2, n))
+    f1, f2 = get_fields(h1, n), get_fields(h2, n)
+    for k in O.FIELDS:
+        assert np.array_equal(f1[k], f2[k]), k
+    if cfg.heat:
+        g1 = s1.g[0]
+        assert np.array_equal(g1, s2.g[0]) and np.abs(g1).max() > 0
