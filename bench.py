@@ -12,8 +12,9 @@ is GLUPS (giga lattice-cell updates per second; the reference prints MLUPS,
 bench.py:23 there). The population buffer (19 x 4 B x 8.4M = 637 MB in FP32)
 is larger than the 129 MB L2, so no flush is needed between steps.
 
-Prints one JSON line. ``value`` is device-timed (CUDA events on the launch
-stream, populations resident in HBM); ``e2e`` runs tack-lbm's application
+Prints one JSON line. ``value`` is device-timed: K steps between two CUDA
+events on the launch stream (quiet steps launched as CUDA graphs of step
+pairs), populations resident in HBM; ``e2e`` runs tack-lbm's application
 loop through the public Solver API (run_lbm.py:207-225: quiet steps, a report
 step and monitors every 10 steps, the coarsened output fields copied to pinned
 host memory, a steering input), timed by the host clock; ``roofline`` is the
@@ -330,26 +331,40 @@ def main():
     world, rank, local, dist, torch = dist_setup(args.gpus)
     import lbm_native as N
     s = make_solver(args.storage, local, args.path)
-    steps = min(args.steps, 4096)
+    steps = args.steps
     for _ in range(args.warmup):
-        s.step()
+        s.step(report=args.report)
     s.sync()
+    # kernel durations for the roofline: a separate pass with every step's
+    # kernels bracketed by CUDA events (lbm_timing)
+    kernel_steps = min(steps, 1000)
     s._h.call("lbm_timing", 1)
+    for _ in range(kernel_steps):
+        s.step(report=args.report)
+    s.sync()
+    t = (ctypes.c_double * 7)()
+    s._h.call("lbm_timing_read", t)
+    s._h.call("lbm_timing", 0)
+
+    # the timed region: K steps between two CUDA events on the launch stream
+    # (lbm_run_timed; quiet steps go as CUDA graphs of step pairs), no events
+    # in between; report steps one lbm_run_timed each, their device times summed
+    def run_timed(count, report_last):
+        ms = ctypes.c_double()
+        s._h.call("lbm_run_timed", int(count), int(report_last), None, ctypes.byref(ms))
+        return ms.value
+
     barrier(dist, torch)
     with Clocks(local) as clocks:
         t0 = time.perf_counter()
         if args.report:
-            for _ in range(steps):
-                s.step(report=True)
+            span_ms = sum(run_timed(1, 1) for _ in range(steps))
         else:
-            s.run(steps)
+            span_ms = run_timed(steps, 0)
         s.sync()
         wall = time.perf_counter() - t0
     barrier(dist, torch)
-    t = (ctypes.c_double * 7)()
-    s._h.call("lbm_timing_read", t)
-    s._h.call("lbm_timing", 0)
-    span_ms = max_over_ranks(t[6], dist, torch)
+    span_ms = max_over_ranks(span_ms, dist, torch)
     cells = s.lat.n
     value = world * cells * steps / (span_ms * 1e-3) / 1e9
     bulk_ms = t[0] / max(t[1], 1)
@@ -410,11 +425,12 @@ def main():
                                  if args.path != "bulkcopy" else None),
                      "traffic_unit": "B per launch (ncu dram read + write)",
                      "kernel": kernel_name, "bytes_per_cell": bytes_cell,
-                     "fluid_cells_per_launch": int(t[2] - solid), "ms_per_launch": bulk_ms},
+                     "fluid_cells_per_launch": int(t[2] - solid), "ms_per_launch": bulk_ms,
+                     "timed_launches": kernel_steps},
         "step_roofline": {"achieved": step_bytes / (span_ms / steps * 1e-3) / 1e9,
                           "frac": step_bytes / (span_ms / steps * 1e-3) / 1e9 / peak,
                           "lid_row_cells": int(t[5])},
-        "gpu_launches": int(t[1]) * (2 if t[5] > 0 else 1),
+        "gpu_launches": steps * (2 if t[5] > 0 else 1) + (steps if args.report else 0),
         "clocks": clocks.summary(),
         "monitors_finite": bool(finite),
         "wall_s": wall,

@@ -238,6 +238,10 @@ lbm_status lbm_managed_free(float *ptr);
 lbm_status lbm_timing(lbm_solver *s, int32_t enable);
 lbm_status lbm_timing_read(lbm_solver *s, double out[7]);
 
+/* lbm_run between two CUDA events on `stream`; *ms = their elapsed time
+ * (synchronous). (No reference counterpart: measurement support.) */
+lbm_status lbm_run_timed(lbm_solver *s, int32_t count, int32_t report_last, void *stream, double *ms);
+
 /* Synchronise the solver's device work (tack.sync, lbm.py:651). */
 lbm_status lbm_sync(lbm_solver *s);
 

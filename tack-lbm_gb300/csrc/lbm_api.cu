@@ -1056,4 +1056,26 @@ lbm_status lbm_vorticity_q(lbm_solver *s, const float *jac, float *vorticity, fl
   return LBM_OK;
 }
 
+lbm_status lbm_run_timed(lbm_solver *s, int32_t count, int32_t report_last, void *stream, double *ms) {
+  LBM_HANDLE(s);
+  if (!ms) return fail(LBM_ERR_ARG, "null output");
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  LBM_CUDA(cudaEventCreate(&ev[0]));
+  cudaError_t e = cudaEventCreate(&ev[1]);
+  if (e == cudaSuccess) e = cudaEventRecord(ev[0], (cudaStream_t)stream);
+  lbm_status st = e == cudaSuccess ? lbm_run(s, count, report_last, stream) : LBM_ERR_CUDA;
+  if (st == LBM_OK) {
+    e = cudaEventRecord(ev[1], (cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+    float t = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, ev[0], ev[1]);
+    *ms = t;
+  }
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  if (st != LBM_OK) return st;
+  if (e != cudaSuccess) return fail(LBM_ERR_CUDA, std::string("lbm_run_timed: ") + cudaGetErrorString(e));
+  return LBM_OK;
+}
+
 }  // extern "C"
