@@ -98,7 +98,11 @@ cudaError_t launch_variant(const Ctx &c, const StepArgs<S> &a, cudaStream_t st, 
                                                                          (int)fblocks);
       cudaEventRecord(c.join, c.side);
     }
-    step_kernel<S, COLL, REPORT, ODD><<<grid, block, 0, st>>>(a);
+    {
+      constexpr int TX = tile_warps_x<S>(), TY = BY / TX;
+      const dim3 tiles((c.cfg.nx + BX * TX - 1) / (BX * TX), (c.cfg.ny + TY - 1) / TY, c.cfg.nz);
+      step_kernel<S, COLL, REPORT, ODD><<<tiles, block, 0, st>>>(a);
+    }
     if (ev) cudaEventRecord(ev[1], st);
     if (gblocks > 0) cudaStreamWaitEvent(st, c.join, 0);
     *rows = 0;
