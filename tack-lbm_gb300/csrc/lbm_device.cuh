@@ -182,8 +182,11 @@ __device__ __forceinline__ float load_l2(const float *p) {
 template <> struct Store<float> {
   using T = float;
   static constexpr bool DEV = false;
-  template <int q> __device__ static float load(const float *p) { return load_l2(p); }
-  template <int q> __device__ static void store(float *p, float v) { __stcs(p, v); }
+  template <int q> __device__ static float load(const float *p) { return *p; }
+  template <int q> __device__ static void store(float *p, float v) { *p = v; }
+  // the same on global memory with the step's hints (any other address space faults)
+  template <int q> __device__ static float gload(const float *p) { return load_l2(p); }
+  template <int q> __device__ static void gstore(float *p, float v) { __stcs(p, v); }
   template <int q> __device__ static double load_value(const float *p) { return (double)*p; }
   template <int q> __device__ static void store_value(float *p, double v) { *p = (float)v; }
 };
@@ -192,14 +195,18 @@ template <> struct Store<double> {
   static constexpr bool DEV = false;
   template <int q> __device__ static double load(const double *p) { return *p; }
   template <int q> __device__ static void store(double *p, double v) { *p = v; }
+  template <int q> __device__ static double gload(const double *p) { return *p; }
+  template <int q> __device__ static void gstore(double *p, double v) { *p = v; }
   template <int q> __device__ static double load_value(const double *p) { return *p; }
   template <int q> __device__ static void store_value(double *p, double v) { *p = v; }
 };
 template <> struct Store<__half> {
   using T = float;
   static constexpr bool DEV = true;
-  template <int q> __device__ static float load(const __half *p) { return __half2float(__ldg(p)); }
-  template <int q> __device__ static void store(__half *p, float d) { __stcs(p, __float2half_rn(d)); }
+  template <int q> __device__ static float load(const __half *p) { return __half2float(*p); }
+  template <int q> __device__ static void store(__half *p, float d) { *p = __float2half_rn(d); }
+  template <int q> __device__ static float gload(const __half *p) { return __half2float(__ldg(p)); }
+  template <int q> __device__ static void gstore(__half *p, float d) { __stcs(p, __float2half_rn(d)); }
   template <int q> __device__ static double load_value(const __half *p) {
     return (double)wq(q) + (double)__half2float(*p);
   }
@@ -210,8 +217,12 @@ template <> struct Store<__half> {
 template <> struct Store<__nv_bfloat16> {
   using T = float;
   static constexpr bool DEV = true;
-  template <int q> __device__ static float load(const __nv_bfloat16 *p) { return __bfloat162float(__ldg(p)); }
-  template <int q> __device__ static void store(__nv_bfloat16 *p, float d) { __stcs(p, __float2bfloat16_rn(d)); }
+  template <int q> __device__ static float load(const __nv_bfloat16 *p) { return __bfloat162float(*p); }
+  template <int q> __device__ static void store(__nv_bfloat16 *p, float d) { *p = __float2bfloat16_rn(d); }
+  template <int q> __device__ static float gload(const __nv_bfloat16 *p) { return __bfloat162float(__ldg(p)); }
+  template <int q> __device__ static void gstore(__nv_bfloat16 *p, float d) {
+    __stcs(p, __float2bfloat16_rn(d));
+  }
   template <int q> __device__ static double load_value(const __nv_bfloat16 *p) {
     return (double)wq(q) + (double)__bfloat162float(*p);
   }
@@ -711,7 +722,7 @@ __device__ __forceinline__ void fast_load(const StepArgs<S> &a, int idx, const O
       S *src = src_loc<q, true>(a, idx, o, r);
       addr = ODD ? (b ? own : src) : (b ? src : own);
     }
-    d[q] = Store<S>::template load<q>(addr);
+    d[q] = Store<S>::template gload<q>(addr);
   });
 }
 
@@ -754,8 +765,8 @@ __device__ __forceinline__ void fast_finish(const StepArgs<S> &a, int x, int y, 
     static_for<Q>([&](auto pc) {
       constexpr int p = decltype(pc)::value;
       // population p moves to x + c_p: the odd-step source location of direction opp(p)
-      if (ODD) Store<S>::template store<p>(src_loc<opp(p), SPECIAL>(a, idx, o, r), d[p]);
-      else Store<S>::template store<p>(a.slot[opp(p)] + idx, d[p]);
+      if (ODD) Store<S>::template gstore<p>(src_loc<opp(p), SPECIAL>(a, idx, o, r), d[p]);
+      else Store<S>::template gstore<p>(a.slot[opp(p)] + idx, d[p]);
     });
   }
   if (REPORT) diagnostics<T>(a.fld, idx, mo, mx, my, mz, prev, v);
@@ -841,12 +852,12 @@ __device__ __forceinline__ void general_cell(const StepArgs<S> &a, int x, int y,
     if (here) {
       // obstacle cell: streamed-in values, or its own w_q on its bounce links
       if (bb) val = rest_value<T, DEV>(q) + wall_term;
-      else val = ODD ? Store<S>::template load<q>(k.L) : Store<S>::template load<q>(a.slot[q] + idx);
+      else val = ODD ? Store<S>::template gload<q>(k.L) : Store<S>::template gload<q>(a.slot[q] + idx);
     } else {
       S *src;
       if (ODD) src = bb ? a.slot[q] + idx : k.L;
       else src = k.wall ? k.L : a.slot[q] + idx;
-      const T got = Store<S>::template load<q>(src);
+      const T got = Store<S>::template gload<q>(src);
       val = bb ? got + wall_term : got;
       if (k.wall) {
         // momentum exchange (lbm.py:429-432); bounced = the population just read
@@ -876,7 +887,7 @@ __device__ __forceinline__ void general_cell(const StepArgs<S> &a, int x, int y,
       } else {
         dst = a.slot[o] + idx;
       }
-      Store<S>::template store<p>(dst, d[p]);
+      Store<S>::template gstore<p>(dst, d[p]);
     });
   }
   if (REPORT) diagnostics<T>(a.fld, idx, m, mx, my, mz, prev, v);
