@@ -20,7 +20,9 @@ step and monitors every 10 steps, the coarsened output fields copied to pinned
 host memory, a steering input), timed by the host clock; ``roofline`` is the
 step kernel's algorithmic bytes (152 B per fluid cell in FP32, 76 B in
 FP16/BF16) over its event-timed duration against the measured HBM copy
-bandwidth; ``adjoint`` times the drag gradient (256x128x32, 2000 steps).
+bandwidth; ``adjoint`` times the drag gradient (256x128x32, 2000 steps);
+``next_rows`` times the temperature step, the flutter and FSI wing steps and
+the derived fields on their own reference workloads (see ``next_rows``).
 
 Under torchrun (N > 1) every rank runs an independent replica on its own GPU
 (the step does not shard: replicas only); rank 0 prints the line.
@@ -299,6 +301,128 @@ def adjoint_timing(device):
             "device_bytes": info["device_bytes"]}
 
 
+# ---------------------------------------------------------------------------
+# the widened rows beside the step: temperature, moving wings, derived fields
+
+def _events(torch):
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def _coupled(step, count, torch):
+    """Host time and device time (events on the legacy stream, which the wing
+    and FSI entry points use) of ``count`` coupled fluid-structure steps."""
+    dev = 0.0
+    a, b = _events(torch)
+    t0 = time.perf_counter()
+    for _ in range(count):
+        a.record()
+        step()
+        b.record()
+        b.synchronize()
+        dev += a.elapsed_time(b)
+    return (time.perf_counter() - t0) * 1e3 / count, dev / count
+
+
+def next_rows(device, peak, torch, solver):
+    """Throughput of the four widened rows on their reference workloads.
+
+    * heat: the heat-sink duct of heat_check.py (320 x 96 x 128, LES at Re 1000,
+      D 12, walls at T = 1), flow step + D3Q7 temperature step, quiet steps as
+      one lbm_run_timed. Bytes per step: every fluid cell 152 B (populations)
+      + 16 B (aux write) + 16 B (aux read); every cell 56 B (7 temperature
+      populations in and out).
+    * flutter: FlutterSolver's default lattice (384 x 192 x 4, LES, Re 500),
+      released, one coupled step per call (the loads come back to the host
+      integrator every step, flutter.py:248-262). 45 MB of populations: the
+      step is L2-resident and launch-bound, so no HBM fraction is given.
+    * fsi: FSISolver's default lattice (256 x 128 x 104, chord 32, span 64,
+      LES, Re 500) with the beam model, released; 152 B per fluid cell plus
+      the 1-byte mask written and read (154 B).
+    * derived: velocity gradient and |curl u| and Q at cell centres on the
+      cylinder run's stride-2 output grid (256 x 128 x 32), 12 B read and 36 B
+      written per point, then 36 B read and 8 B written per cell.
+    """
+    import ctypes as C
+    import lbm
+    import flutter
+    import fsi
+    rows = {}
+
+    s = lbm.Solver(320, 96, 128, collision="les", obstacle="heatsink", reynolds=1000.0, heat=True,
+                   diameter=12.0, device=f"cuda:{device}")
+    s.set_wall_temperature(1.0)
+    ms = C.c_double()
+    s._h.call("lbm_run_timed", 50, 1, None, C.byref(ms))
+    steps = 400
+    s._h.call("lbm_run_timed", steps, 0, None, C.byref(ms))
+    n = s.lat.n
+    fluid = n - int(s.mask().sum())
+    byts = fluid * (152 + 16 + 16) + n * 56
+    per = ms.value / steps
+    m = s.monitors(100)
+    rows["heat"] = {"workload": "heat-sink duct, LES Re 1000, D3Q7 temperature, 320x96x128, quiet steps",
+                    "glups": n / (per * 1e-3) / 1e9, "ms_per_step": per, "bytes_per_step": byts,
+                    "achieved_gbs": byts / (per * 1e-3) / 1e9, "frac": byts / (per * 1e-3) / 1e9 / peak,
+                    "finite": bool(np.isfinite(list(m.values())).all())}
+    del s
+
+    w = flutter.FlutterSolver(384, 192, 4, device=f"cuda:{device}")
+    w.release()
+    for _ in range(20):
+        w.step()
+    host_ms, dev_ms = _coupled(w.step, 500, torch)
+    n = 384 * 192 * 4
+    rows["flutter"] = {"workload": "pitch-plunge NACA 0012, LES Re 500, 384x192x4, coupled steps",
+                       "glups": n / (host_ms * 1e-3) / 1e9, "host_ms_per_step": host_ms,
+                       "device_ms_per_step": dev_ms, "finite": bool(np.isfinite(w.coefficients()).all())}
+    del w
+
+    f = fsi.FSISolver(device=f"cuda:{device}")
+    f.release()
+    for _ in range(5):
+        f.step()
+    host_ms, dev_ms = _coupled(f.step, 100, torch)
+    n = f.lat.n
+    fluid = n - int(f.mask().sum())
+    byts = fluid * 152 + 2 * n
+    rows["fsi"] = {"workload": "cantilever wing, beam model, LES Re 500, 256x128x104, coupled steps",
+                   "glups": n / (host_ms * 1e-3) / 1e9, "host_ms_per_step": host_ms,
+                   "device_ms_per_step": dev_ms, "bytes_per_step": byts,
+                   "achieved_gbs": byts / (dev_ms * 1e-3) / 1e9, "frac": byts / (dev_ms * 1e-3) / 1e9 / peak,
+                   "finite": bool(np.isfinite(f.coefficients()).all())}
+    del f
+
+    solver.update_output()
+    mx, my, mz = solver.out_dims
+    pts, cells = mx * my * mz, (mx - 1) * (my - 1) * (mz - 1)
+    dev = torch.device(f"cuda:{device}")
+    jac = torch.empty(9 * pts, dtype=torch.float32, device=dev)
+    vort = torch.empty(cells, dtype=torch.float32, device=dev)
+    q = torch.empty(cells, dtype=torch.float32, device=dev)
+    inv_h = solver.diameter / solver.stride
+
+    def derive():
+        solver._h.call("lbm_velocity_gradient", C.c_void_p(jac.data_ptr()), float(inv_h), None)
+        solver._h.call("lbm_vorticity_q", C.c_void_p(jac.data_ptr()), C.c_void_p(vort.data_ptr()),
+                       C.c_void_p(q.data_ptr()), 1, None)
+
+    for _ in range(3):
+        derive()
+    a, b = _events(torch)
+    a.record()
+    reps = 50
+    for _ in range(reps):
+        derive()
+    b.record()
+    b.synchronize()
+    per = a.elapsed_time(b) / reps
+    byts = pts * (12 + 36) + cells * (36 + 8)
+    rows["derived"] = {"workload": f"velocity gradient + vorticity + Q at cells, {mx}x{my}x{mz} output grid",
+                       "ms_per_call": per, "bytes": byts, "achieved_gbs": byts / (per * 1e-3) / 1e9,
+                       "frac": byts / (per * 1e-3) / 1e9 / peak}
+    return rows
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -317,6 +441,8 @@ def main():
     ap.add_argument("--study-steps", type=int, default=None)
     ap.add_argument("--no-adjoint", action="store_true",
                     help="skip the drag-adjoint timing (256x128x32, 2000 steps, FP32)")
+    ap.add_argument("--no-next-rows", action="store_true",
+                    help="skip the heat, flutter, FSI and derived-field timings")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -438,6 +564,8 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         f = s.populations(np.float32)
         line["cpu_baseline"] = cpu_baseline_single(f)
+    if world == 1 and not args.no_next_rows:
+        line["next_rows"] = next_rows(local, peak, torch_host, s)
     if not args.no_adjoint:
         del s
         line["adjoint"] = adjoint_timing(local)

@@ -11,12 +11,13 @@ z = span, with inflow at x = 0 and an outflow at x = nx - 1. Every step:
   the modal state, through moving-wall bounce-back, second order on wetted
   links (interpolated bounce-back).
 
-The structural model comes from the caller (``fem=``): an object with the
-modal frequencies ``omega0``, the modal plunge and twist along the span
-``h[k, :]`` and ``alpha[k, :]`` (the last column at the tip) and
-``sections_at(z)`` giving the modes' plunge and twist at heights z. The
-reference builds it with MFEM (fsi_beam.WingBeam), which this package does
-not ship. ``Modal`` integrates the modal equations as the reference does.
+The structural model is any object with the modal frequencies ``omega0``,
+the modal plunge and twist along the span ``h[k, :]`` and ``alpha[k, :]``
+(the last column at the tip) and ``sections_at(z)`` giving the modes'
+plunge and twist at heights z. By default it is ``fsi_beam.WingBeam``, the
+reference's bending-torsion beam, here assembled with this package's own
+1-D finite elements instead of MFEM. ``Modal`` integrates the modal
+equations as the reference does.
 """
 
 import ctypes
@@ -132,8 +133,8 @@ def fsi_step(lat, phys, geo, flow, diag, f_in, f_out, device=0):
 
 
 class FSISolver:
-    """tack-lbm's FSISolver (fsi.py:189-325) on the GB300 FSI kernel, with the
-    caller's modal model ``fem`` (see the module docstring)."""
+    """tack-lbm's FSISolver (fsi.py:189-325) on the GB300 FSI kernel; ``fem``
+    defaults to ``fsi_beam.WingBeam(chord, span, ea)`` as there (fsi.py:194)."""
 
     OUTPUT = _OUT
 
@@ -142,8 +143,8 @@ class FSISolver:
                  fem=None):
         from lbm import D3Q19, Flow
         if fem is None:
-            raise NotImplementedError("the default structural model (fsi_beam.WingBeam) needs MFEM; "
-                                      "pass fem= a modal model (omega0, h, alpha, sections_at)")
+            from fsi_beam import WingBeam
+            fem = WingBeam(chord=chord, span=span, ea=ea)
         self.device_index = 0 if device in ("cuda", None) else int(str(device).split(":")[-1])
         self.nx, self.ny, self.nz = nx, ny, nz
         self.lat = D3Q19(nx, ny, nz)

@@ -92,3 +92,39 @@ def test_fsi_solver_against_oracle():
     assert np.isfinite(s.coefficients()).all()
     tip_h, tip_a = s.tip()
     assert np.isfinite([tip_h, tip_a]).all()
+
+
+def test_fsi_solver_default_beam():
+    """FSISolver with no fem= builds the bending-torsion beam (fsi.py:194) and
+    couples it: the released wing's kinematics, masks and loads follow the
+    oracle stepped with the same modal integrator."""
+    import fsi
+    from fsi_beam import WingBeam
+    s = fsi.FSISolver(48, 24, 8, chord=12.0, span=5.5, ea=0.4, u0=0.06, reynolds=150.0, collision="les",
+                      reduced_velocity=3.0, damping=0.01, hardening=50.0)
+    beam = WingBeam(chord=12.0, span=5.5, ea=0.4)
+    assert np.array_equal(s.fem.omega0, beam.omega0)
+    k = s.torsion
+    assert abs(beam.alpha[k, -1]) * 6.0 > abs(beam.h[k, -1])  # the first twist-dominated mode
+    ref = fsi.Modal(beam, s.structure.omega, damping=0.01, hardening=50.0, torsion=k)
+    cfg = FS.FsiConfig(48, 24, 8, 12.0, 12.0, 12.0, 0.4, 5.5, kin=np.zeros((8, 4)), collision="les", nu=s.nu,
+                       u0=0.06, sponge_start=36.0, sponge_strength=1.0)
+    idx = np.arange(cfg.n)
+    f = s.populations().astype(np.float64)
+    s.release()
+    ref.v[k] += np.radians(2.0) * ref.omega[k] / beam.alpha[k, -1]
+    mh, ma = beam.sections_at(np.arange(8) + 0.5)
+    for step in range(6):
+        cfg.kin = np.stack([ref.q @ mh, ref.q @ ma, ref.v @ mh, ref.v @ ma], 1)
+        assert np.allclose(s._kin, cfg.kin, rtol=1e-9, atol=1e-15), f"step {step + 1}"
+        mask = FS.solid(cfg, idx % cfg.nx, (idx // cfg.nx) % cfg.ny, idx // (cfg.nx * cfg.ny))
+        assert np.array_equal(s.mask(), mask.astype(np.uint8)), f"step {step + 1}"
+        s.step()
+        f, load = FS.step(cfg, f)
+        f = f.reshape(-1)
+        load = load.copy()
+        load[:, 2] *= -1.0
+        ref.step(mh @ load[:, 1] + ma @ load[:, 2])
+        assert O.weight_err(s.populations(), f) <= 6e-6, f"step {step + 1}"
+        assert np.abs(s.layer_load - load).max() <= 1e-4 * max(1e-3, np.abs(load).max()), f"step {step + 1}"
+    assert abs(s.tip()[1]) > 0.0
