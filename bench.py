@@ -323,31 +323,17 @@ def _coupled(step, count, torch):
     return (time.perf_counter() - t0) * 1e3 / count, dev / count
 
 
-def next_rows(device, peak, torch, solver):
-    """Throughput of the four widened rows on their reference workloads.
+NEXT_ROWS = ("heat", "flutter", "fsi", "derived")
 
-    * heat: the heat-sink duct of heat_check.py (320 x 96 x 128, LES at Re 1000,
-      D 12, walls at T = 1), flow step + D3Q7 temperature step, quiet steps as
-      one lbm_run_timed. Bytes per step: every fluid cell 152 B (populations)
-      + 16 B (aux write) + 16 B (aux read); every cell 56 B (7 temperature
-      populations in and out).
-    * flutter: FlutterSolver's default lattice (384 x 192 x 4, LES, Re 500),
-      released, one coupled step per call (the loads come back to the host
-      integrator every step, flutter.py:248-262). 45 MB of populations: the
-      step is L2-resident and launch-bound, so no HBM fraction is given.
-    * fsi: FSISolver's default lattice (256 x 128 x 104, chord 32, span 64,
-      LES, Re 500) with the beam model, released; 152 B per fluid cell plus
-      the 1-byte mask written and read (154 B).
-    * derived: velocity gradient and |curl u| and Q at cell centres on the
-      cylinder run's stride-2 output grid (256 x 128 x 32), 12 B read and 36 B
-      written per point, then 36 B read and 8 B written per cell.
-    """
+
+def row_heat(device, peak, torch):
+    """The heat-sink duct of heat_check.py (320 x 96 x 128, LES at Re 1000, D 12,
+    walls at T = 1): flow step + D3Q7 temperature step, quiet steps as one
+    lbm_run_timed. Bytes per step: every fluid cell 152 B (populations) + 16 B
+    (aux write) + 16 B (aux read); every cell 56 B (7 temperature populations
+    in and out)."""
     import ctypes as C
     import lbm
-    import flutter
-    import fsi
-    rows = {}
-
     s = lbm.Solver(320, 96, 128, collision="les", obstacle="heatsink", reynolds=1000.0, heat=True,
                    diameter=12.0, device=f"cuda:{device}")
     s.set_wall_temperature(1.0)
@@ -360,23 +346,34 @@ def next_rows(device, peak, torch, solver):
     byts = fluid * (152 + 16 + 16) + n * 56
     per = ms.value / steps
     m = s.monitors(100)
-    rows["heat"] = {"workload": "heat-sink duct, LES Re 1000, D3Q7 temperature, 320x96x128, quiet steps",
-                    "glups": n / (per * 1e-3) / 1e9, "ms_per_step": per, "bytes_per_step": byts,
-                    "achieved_gbs": byts / (per * 1e-3) / 1e9, "frac": byts / (per * 1e-3) / 1e9 / peak,
-                    "finite": bool(np.isfinite(list(m.values())).all())}
-    del s
+    return {"workload": "heat-sink duct, LES Re 1000, D3Q7 temperature, 320x96x128, quiet steps",
+            "glups": n / (per * 1e-3) / 1e9, "ms_per_step": per, "bytes_per_step": byts,
+            "achieved_gbs": byts / (per * 1e-3) / 1e9, "frac": byts / (per * 1e-3) / 1e9 / peak,
+            "finite": bool(np.isfinite(list(m.values())).all())}
 
+
+def row_flutter(device, peak, torch):
+    """FlutterSolver's default lattice (384 x 192 x 4, LES, Re 500), released,
+    one coupled step per call (the loads come back to the host integrator
+    every step, flutter.py:248-262). 45 MB of populations: the step is
+    L2-resident and launch-bound, so no HBM fraction is given."""
+    import flutter
     w = flutter.FlutterSolver(384, 192, 4, device=f"cuda:{device}")
     w.release()
     for _ in range(20):
         w.step()
     host_ms, dev_ms = _coupled(w.step, 500, torch)
     n = 384 * 192 * 4
-    rows["flutter"] = {"workload": "pitch-plunge NACA 0012, LES Re 500, 384x192x4, coupled steps",
-                       "glups": n / (host_ms * 1e-3) / 1e9, "host_ms_per_step": host_ms,
-                       "device_ms_per_step": dev_ms, "finite": bool(np.isfinite(w.coefficients()).all())}
-    del w
+    return {"workload": "pitch-plunge NACA 0012, LES Re 500, 384x192x4, coupled steps",
+            "glups": n / (host_ms * 1e-3) / 1e9, "host_ms_per_step": host_ms,
+            "device_ms_per_step": dev_ms, "finite": bool(np.isfinite(w.coefficients()).all())}
 
+
+def row_fsi(device, peak, torch):
+    """FSISolver's default lattice (256 x 128 x 104, chord 32, span 64, LES,
+    Re 500) with the beam model, released: 152 B per fluid cell plus the
+    1-byte mask written and read (154 B)."""
+    import fsi
     f = fsi.FSISolver(device=f"cuda:{device}")
     f.release()
     for _ in range(5):
@@ -385,13 +382,18 @@ def next_rows(device, peak, torch, solver):
     n = f.lat.n
     fluid = n - int(f.mask().sum())
     byts = fluid * 152 + 2 * n
-    rows["fsi"] = {"workload": "cantilever wing, beam model, LES Re 500, 256x128x104, coupled steps",
-                   "glups": n / (host_ms * 1e-3) / 1e9, "host_ms_per_step": host_ms,
-                   "device_ms_per_step": dev_ms, "bytes_per_step": byts,
-                   "achieved_gbs": byts / (dev_ms * 1e-3) / 1e9, "frac": byts / (dev_ms * 1e-3) / 1e9 / peak,
-                   "finite": bool(np.isfinite(f.coefficients()).all())}
-    del f
+    return {"workload": "cantilever wing, beam model, LES Re 500, 256x128x104, coupled steps",
+            "glups": n / (host_ms * 1e-3) / 1e9, "host_ms_per_step": host_ms,
+            "device_ms_per_step": dev_ms, "bytes_per_step": byts,
+            "achieved_gbs": byts / (dev_ms * 1e-3) / 1e9, "frac": byts / (dev_ms * 1e-3) / 1e9 / peak,
+            "finite": bool(np.isfinite(f.coefficients()).all())}
 
+
+def row_derived(device, peak, torch, solver):
+    """Velocity gradient, then |curl u| and Q at cell centres, on the cylinder
+    run's stride-2 output grid (256 x 128 x 32): 12 B read and 36 B written
+    per point, then 36 B read and 8 B written per cell."""
+    import ctypes as C
     solver.update_output()
     mx, my, mz = solver.out_dims
     pts, cells = mx * my * mz, (mx - 1) * (my - 1) * (mz - 1)
@@ -417,10 +419,20 @@ def next_rows(device, peak, torch, solver):
     b.synchronize()
     per = a.elapsed_time(b) / reps
     byts = pts * (12 + 36) + cells * (36 + 8)
-    rows["derived"] = {"workload": f"velocity gradient + vorticity + Q at cells, {mx}x{my}x{mz} output grid",
-                       "ms_per_call": per, "bytes": byts, "achieved_gbs": byts / (per * 1e-3) / 1e9,
-                       "frac": byts / (per * 1e-3) / 1e9 / peak}
-    return rows
+    return {"workload": f"velocity gradient + vorticity + Q at cells, {mx}x{my}x{mz} output grid",
+            "ms_per_call": per, "bytes": byts, "achieved_gbs": byts / (per * 1e-3) / 1e9,
+            "frac": byts / (per * 1e-3) / 1e9 / peak}
+
+
+def next_rows(device, peak, torch, solver, rows=NEXT_ROWS):
+    """Throughput of the widened rows on their reference workloads (row_*)."""
+    out = {}
+    for name in rows:
+        if name == "derived":
+            out[name] = row_derived(device, peak, torch, solver)
+        else:
+            out[name] = {"heat": row_heat, "flutter": row_flutter, "fsi": row_fsi}[name](device, peak, torch)
+    return out
 
 
 def main():
@@ -443,6 +455,9 @@ def main():
                     help="skip the drag-adjoint timing (256x128x32, 2000 steps, FP32)")
     ap.add_argument("--no-next-rows", action="store_true",
                     help="skip the heat, flutter, FSI and derived-field timings")
+    ap.add_argument("--next-rows-only", default=None, metavar="ROWS",
+                    help="time only these widened rows (comma list of heat,flutter,fsi,derived) and print "
+                         "one JSON line with them")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -456,6 +471,16 @@ def main():
 
     world, rank, local, dist, torch = dist_setup(args.gpus)
     import lbm_native as N
+    if args.next_rows_only:
+        import torch as torch_host
+        rows = [r.strip() for r in args.next_rows_only.split(",") if r.strip()]
+        bad = [r for r in rows if r not in NEXT_ROWS]
+        if bad:
+            ap.error(f"unknown rows {bad}; choose from {NEXT_ROWS}")
+        s = make_solver(args.storage, local, args.path) if "derived" in rows else None
+        peak, _ = peaks()
+        print(json.dumps({"next_rows": next_rows(local, peak, torch_host, s, rows)}), flush=True)
+        return 0
     s = make_solver(args.storage, local, args.path)
     steps = args.steps
     for _ in range(args.warmup):

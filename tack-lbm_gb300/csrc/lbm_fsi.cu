@@ -3,8 +3,9 @@
 // An elastic NACA 0012 wing from the root plane (a mirror below z = 0) to
 // z = span: every lattice layer z has its own plunge h, pitch alpha and their
 // rates, given by the caller's structural model each step. Per step:
-//   * fsi_mask_kernel evaluates each cell's layer section test in float64
-//     into a byte mask (fsi.py:35-47);
+//   * fsi_mask_kernel evaluates each cell's layer section test into a byte
+//     mask (fsi.py:35-47): float64 results, with a float32 prefilter that
+//     decides the points away from the outline (lbm_naca.cuh);
 //   * fsi_step_kernel (float32 populations on A/B buffers f[q*n + idx]):
 //     inflow at x = 0 from the free-stream equilibrium, zero-gradient outflow
 //     at x = nx - 1, periodic y, mirror planes below z = 0 and above
@@ -25,6 +26,7 @@
 
 #include "lbm_device.cuh"
 #include "lbm_host.h"
+#include "lbm_naca.cuh"
 
 namespace lbmf {
 
@@ -38,6 +40,8 @@ struct FsiArgs {
   float *fout;
   const uint8_t *mask;
   const double *kin;
+  const NacaF *naca;   // per layer: the float32 prefilter (reach < 0 past the span)
+  const float4 *kinf;  // per layer: h, dh/dt, dalpha/dt as float32
   double *load;  // 3 per layer
   float *fld[5];
   int nx, ny, nz, n;
@@ -46,7 +50,7 @@ struct FsiArgs {
   float omega_bgk, tau0, smag_c, magic;
 };
 
-__device__ __forceinline__ bool section(const FsiArgs &a, double x, double y, int z) {
+__device__ __forceinline__ bool section64(const FsiArgs &a, double x, double y, int z) {
   const double *k = a.kin + KIN * z;
   const double dx = x - a.x_ea, dy = y - (a.y_ea + k[0]);
   const double s = dx * k[4] - dy * k[5], t = dx * k[5] + dy * k[4];
@@ -57,10 +61,16 @@ __device__ __forceinline__ bool section(const FsiArgs &a, double x, double y, in
   return xc >= 0.0 && xc <= 1.0 && fabs(t) < half && (double)z + 0.5 < a.span;
 }
 
+// the section test at (xf, yf) = (x, y) exactly representable in float32
+__device__ __forceinline__ bool section(const FsiArgs &a, float xf, float yf, double x, double y, int z) {
+  const int r = naca_prefilter(a.naca[z], xf, yf);
+  return r != 0 ? r > 0 : section64(a, x, y, z);
+}
+
 __global__ void fsi_mask_kernel(const __grid_constant__ FsiArgs a, uint8_t *mask) {
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < a.n; idx += gridDim.x * blockDim.x) {
     const int x = idx % a.nx, y = (idx / a.nx) % a.ny, z = idx / (a.nx * a.ny);
-    mask[idx] = section(a, (double)x, (double)y, z) ? 1 : 0;
+    mask[idx] = section(a, (float)x, (float)y, (double)x, (double)y, z) ? 1 : 0;
   }
 }
 
@@ -68,8 +78,10 @@ __global__ void fsi_mask_kernel(const __grid_constant__ FsiArgs a, uint8_t *mask
 __device__ __forceinline__ double wall_fraction(const FsiArgs &a, int x, int y, int z, int cxq, int cyq, int zs) {
   double lo = 0.0, hi = 1.0;
   for (int it = 0; it < 6; ++it) {
-    const double mid = 0.5 * (lo + hi);
-    const bool in = section(a, (double)x - mid * cxq, (double)y - mid * cyq, mid >= 0.5 ? zs : z);
+    const double mid = 0.5 * (lo + hi);  // k / 64: the offsets below are exact in float32
+    const float mf = (float)mid;
+    const bool in = section(a, (float)x - mf * (float)cxq, (float)y - mf * (float)cyq, (double)x - mid * cxq,
+                            (double)y - mid * cyq, mid >= 0.5 ? zs : z);
     if (in) hi = mid;
     else lo = mid;
   }
@@ -83,7 +95,7 @@ __global__ void __launch_bounds__(BX * BY) fsi_step_kernel(const __grid_constant
   if (x < a.nx && y < a.ny) {
     const int idx = (z * a.ny + y) * a.nx + x;
     const bool here = a.mask[idx] != 0;
-    const float hz = (float)a.kin[KIN * z];
+    const float hz = a.kinf[z].x;
     float d[Q];
     static_for<Q>([&](auto qc) {
       constexpr int q = decltype(qc)::value;
@@ -108,8 +120,8 @@ __global__ void __launch_bounds__(BX * BY) fsi_step_kernel(const __grid_constant
       float val = pulled;
       if (a.mask[src]) {
         const float bounced = a.fin[(size_t)o * a.n + idx];
-        const double *k = a.kin + KIN * zs;
-        const float kh = (float)k[0], kdh = (float)k[2], kda = (float)k[3];
+        const float4 k = a.kinf[zs];
+        const float kh = k.x, kdh = k.y, kda = k.z;
         float px = (float)x - 0.5f * (float)cx(q), py = (float)y - 0.5f * (float)cy(q);
         float cu = (float)cx(q) * (kda * (py - (float)a.y_ea - kh)) + (float)cy(q) * (kdh - kda * (px - (float)a.x_ea));
         float back = bounced + 6.f * wq(q) * cu;
@@ -155,9 +167,9 @@ __global__ void __launch_bounds__(BX * BY) fsi_step_kernel(const __grid_constant
     collide<float, COLL, false>(post, mo, pr, a.omega_bgk, a.tau0, a.smag_c, a.magic);
     const float t = fmaxf(0.f, ((float)x - a.sponge_start) * a.inv_sponge_len);
     const float sigma = here ? 1.f : a.sponge_strength * t * t;
-    const double *k = a.kin + KIN * z;
-    const float wx = (float)k[3] * ((float)y - (float)a.y_ea - (float)k[0]);
-    const float wy = (float)k[2] - (float)k[3] * ((float)x - (float)a.x_ea);
+    const float4 k = a.kinf[z];
+    const float wx = k.z * ((float)y - (float)a.y_ea - k.x);
+    const float wy = k.y - k.z * ((float)x - (float)a.x_ea);
     const float rho_s = mo.rho + sigma * (1.f - mo.rho);
     const float usx = here ? wx : mo.ux, usy = here ? wy : mo.uy, usz = here ? 0.f : mo.uz;
     float e0[Q], e1[Q];
@@ -218,7 +230,7 @@ struct lbm_fsi {
   float *f[2] = {nullptr, nullptr};
   int cur = 0;
   uint8_t *mask = nullptr;
-  double *kin = nullptr;
+  double *kin = nullptr;  // one buffer: KIN doubles, a float4 and a NacaF per layer
   double *load = nullptr;
   float *fld[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   int stride = 1;
@@ -272,6 +284,8 @@ lbmf::FsiArgs fargs(const lbm_fsi *w) {
   lbmf::FsiArgs a{};
   a.mask = w->mask;
   a.kin = w->kin;
+  a.kinf = reinterpret_cast<const float4 *>(w->kin + lbmf::KIN * c.nz);
+  a.naca = reinterpret_cast<const lbmk::NacaF *>(a.kinf + c.nz);
   a.load = w->load;
   for (int k = 0; k < 5; ++k) a.fld[k] = w->fld[k];
   a.nx = c.nx;
@@ -294,15 +308,27 @@ lbmf::FsiArgs fargs(const lbm_fsi *w) {
   return a;
 }
 
-// upload the layer kinematics (with cos, sin of each pitch) and build the mask
+size_t kin_bytes(int nz) { return (size_t)nz * (lbmf::KIN * sizeof(double) + sizeof(float4) + sizeof(lbmk::NacaF)); }
+
+// upload the layer kinematics (with cos, sin of each pitch, their float32
+// copies and the section prefilter's inputs) and build the mask
 lbm_status set_kin(lbm_fsi *w, const double *kin) {
-  std::vector<double> k((size_t)lbmf::KIN * w->cfg.nz);
-  for (int z = 0; z < w->cfg.nz; ++z) {
+  const lbm_fsi_config &c = w->cfg;
+  const int nz = c.nz;
+  std::vector<unsigned char> buf(kin_bytes(nz));
+  double *k = reinterpret_cast<double *>(buf.data());
+  float4 *kf = reinterpret_cast<float4 *>(k + lbmf::KIN * nz);
+  lbmk::NacaF *nf = reinterpret_cast<lbmk::NacaF *>(kf + nz);
+  for (int z = 0; z < nz; ++z) {
     for (int j = 0; j < 4; ++j) k[lbmf::KIN * z + j] = kin[4 * z + j];
     k[lbmf::KIN * z + 4] = std::cos(kin[4 * z + 1]);
     k[lbmf::KIN * z + 5] = std::sin(kin[4 * z + 1]);
+    kf[z] = make_float4((float)kin[4 * z], (float)kin[4 * z + 2], (float)kin[4 * z + 3], 0.f);
+    nf[z] = lbmk::make_naca_f(c.chord, c.x_ea, c.y_ea + kin[4 * z], c.ea, k[lbmf::KIN * z + 4],
+                              k[lbmf::KIN * z + 5]);
+    if (!((double)z + 0.5 < c.span)) nf[z].reach = -1.f;  // past the tip: no section
   }
-  FCUDA(cudaMemcpy(w->kin, k.data(), k.size() * sizeof(double), cudaMemcpyHostToDevice));
+  FCUDA(cudaMemcpy(w->kin, buf.data(), buf.size(), cudaMemcpyHostToDevice));
   lbmf::fsi_mask_kernel<<<lbmk::cell_grid(w->n), 256>>>(fargs(w), w->mask);
   FCUDA(cudaGetLastError());
   return LBM_OK;
@@ -347,8 +373,8 @@ lbm_status lbm_fsi_create(const lbm_fsi_config *cfg, lbm_fsi **out) {
   cudaError_t e = cudaMalloc(&w->f[0], fb);
   if (e == cudaSuccess) e = cudaMalloc(&w->f[1], fb);
   if (e == cudaSuccess) e = cudaMalloc(&w->mask, (size_t)w->n);
-  if (e == cudaSuccess) e = cudaMalloc(&w->kin, (size_t)lbmf::KIN * cfg->nz * sizeof(double));
-  if (e == cudaSuccess) e = cudaMemset(w->kin, 0, (size_t)lbmf::KIN * cfg->nz * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&w->kin, kin_bytes(cfg->nz));
+  if (e == cudaSuccess) e = cudaMemset(w->kin, 0, kin_bytes(cfg->nz));
   if (e == cudaSuccess) e = cudaMalloc(&w->load, (size_t)3 * cfg->nz * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&w->ptrs, 10 * sizeof(float *));
   for (int k = 0; k < 5 && e == cudaSuccess; ++k) {

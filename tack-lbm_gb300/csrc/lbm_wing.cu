@@ -4,7 +4,8 @@
 // about its elastic axis; the structure (integrated on the host) and the
 // fluid exchange data every step. Per step:
 //   * wing_mask_kernel evaluates the section test (flutter.py:30-42) once per
-//     cell in float64 into a byte mask, so the mask is exact at any state and
+//     cell into a byte mask with float64 results (a float32 prefilter decides
+//     the cells away from the outline, lbm_naca.cuh), so the mask is exact and
 //     the step kernel's 19 source tests are byte loads (mostly L1 hits);
 //   * wing_step_kernel (float32, A/B buffers f[q*n + idx], one thread per
 //     cell, periodic in x, y and z) pulls the populations, applies halfway
@@ -25,6 +26,7 @@
 
 #include "lbm_device.cuh"
 #include "lbm_host.h"
+#include "lbm_naca.cuh"
 
 namespace lbmw {
 
@@ -42,11 +44,16 @@ struct WingArgs {
   float omega_bgk, tau0, smag_c, magic;
 };
 
-// the section test of flutter.py:30-42 in float64
-__global__ void wing_mask_kernel(uint8_t *mask, int nx, int ny, int n, double chord, double x_ea, double y_ea,
-                                 double ea, double h, double ca, double sa) {
+// the section test of flutter.py:30-42 in float64, after the float32 prefilter
+__global__ void wing_mask_kernel(uint8_t *mask, int nx, int ny, int n, NacaF nf, double chord, double x_ea,
+                                 double y_ea, double ea, double h, double ca, double sa) {
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
     const int x = idx % nx, y = (idx / nx) % ny;
+    const int r = naca_prefilter(nf, (float)x, (float)y);
+    if (r != 0) {
+      mask[idx] = r > 0 ? 1 : 0;
+      continue;
+    }
     const double dx = (double)x - x_ea, dy = (double)y - (y_ea + h);
     const double s = dx * ca - dy * sa, t = dx * sa + dy * ca;
     const double xc = s / chord + ea;
@@ -213,8 +220,10 @@ void wrelease(lbm_wing *w) {
 
 lbm_status build_mask(lbm_wing *w, const double st[4]) {
   const lbm_wing_config &c = w->cfg;
-  lbmw::wing_mask_kernel<<<lbmk::cell_grid(w->n), 256>>>(w->mask, c.nx, c.ny, (int)w->n, c.chord, c.x_ea, c.y_ea,
-                                                         c.ea, st[0], std::cos(st[1]), std::sin(st[1]));
+  const double ca = std::cos(st[1]), sa = std::sin(st[1]);
+  const lbmk::NacaF nf = lbmk::make_naca_f(c.chord, c.x_ea, c.y_ea + st[0], c.ea, ca, sa);
+  lbmw::wing_mask_kernel<<<lbmk::cell_grid(w->n), 256>>>(w->mask, c.nx, c.ny, (int)w->n, nf, c.chord, c.x_ea,
+                                                         c.y_ea, c.ea, st[0], ca, sa);
   WCUDA(cudaGetLastError());
   return LBM_OK;
 }
