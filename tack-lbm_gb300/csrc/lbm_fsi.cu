@@ -88,6 +88,50 @@ __device__ __forceinline__ double wall_fraction(const FsiArgs &a, int x, int y, 
   return 0.5 * (lo + hi);
 }
 
+// The interpolated bounce-back of one wetted link, a fluid cell (x, y, z)
+// whose source (x - c_q, zs) lies in the wing (fsi.py:110-135): the wall's
+// place on the link by bisection, the bounced value (far-wall form for
+// delta >= 1/2, near-wall form with the cell behind otherwise) and the
+// link's momentum exchange added to (fx, fy, mz). Out of line on purpose:
+// few links are wetted, and inlining the bisection with its float64
+// fallback into all 18 directions bloats the kernel's common path.
+__device__ __noinline__ float wetted_link(const FsiArgs &a, int x, int y, int z, int zs, int idx, int q, int o,
+                                          int cxq, int cyq, int czq, float w, float bounced, float &fx, float &fy,
+                                          float &mz) {
+  const float4 k = a.kinf[zs];
+  const float kh = k.x, kdh = k.y, kda = k.z;
+  const double delta = wall_fraction(a, x, y, z, cxq, cyq, zs);
+  const float df = (float)delta;
+  const float px = (float)x - df * (float)cxq, py = (float)y - df * (float)cyq;
+  const float cu = (float)cxq * (kda * (py - (float)a.y_ea - kh)) + (float)cyq * (kdh - kda * (px - (float)a.x_ea));
+  float back = bounced + 6.f * w * ((float)cxq * (kda * ((float)y - 0.5f * (float)cyq - (float)a.y_ea - kh)) +
+                                    (float)cyq * (kdh - kda * ((float)x - 0.5f * (float)cxq - (float)a.x_ea)));
+  if (delta >= 0.5) {
+    back = (bounced + (2.f * df - 1.f) * a.fin[(size_t)q * a.n + idx] + 6.f * w * cu) / (2.f * df);
+  } else {
+    int xn = x + cxq;
+    xn += xn < 0 ? a.nx : 0;
+    xn -= xn >= a.nx ? a.nx : 0;
+    int yn = y + cyq;
+    yn += yn < 0 ? a.ny : 0;
+    yn -= yn >= a.ny ? a.ny : 0;
+    const int zn = z + czq;
+    const int zc = zn < 0 ? 0 : (zn > a.nz - 1 ? a.nz - 1 : zn);
+    const int nidx = (zc * a.ny + yn) * a.nx + xn;
+    if (zn == zc && !a.mask[nidx]) {
+      const float behind = a.fin[(size_t)o * a.n + nidx];
+      back = 2.f * df * bounced + (1.f - 2.f * df) * behind + 6.f * w * cu;
+    }
+  }
+  // momentum exchange relative to the fluid at rest
+  const float hit = bounced + back - 2.f * w;
+  const float dfx = hit * (float)(-cxq), dfy = hit * (float)(-cyq);
+  fx += dfx;
+  fy += dfy;
+  mz += (px - (float)a.x_ea) * dfy - (py - (float)a.y_ea - a.kinf[z].x) * dfx;
+  return back;
+}
+
 template <int COLL, bool REPORT>
 __global__ void __launch_bounds__(BX * BY) fsi_step_kernel(const __grid_constant__ FsiArgs a) {
   const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
@@ -115,7 +159,7 @@ __global__ void __launch_bounds__(BX * BY) fsi_step_kernel(const __grid_constant
         pulled = wq(q) * (1.f + 3.f * (float)cx(q) * a.u0 + 4.5f * (float)(cx(q) * cx(q)) * a.u0 * a.u0 -
                           1.5f * a.u0 * a.u0);
       } else {
-        pulled = a.fin[(size_t)(flip ? mq : q) * a.n + src];
+        pulled = load_l2(a.fin + (size_t)(flip ? mq : q) * a.n + src);
       }
       float val = pulled;
       if (a.mask[src]) {
@@ -125,36 +169,7 @@ __global__ void __launch_bounds__(BX * BY) fsi_step_kernel(const __grid_constant
         float px = (float)x - 0.5f * (float)cx(q), py = (float)y - 0.5f * (float)cy(q);
         float cu = (float)cx(q) * (kda * (py - (float)a.y_ea - kh)) + (float)cy(q) * (kdh - kda * (px - (float)a.x_ea));
         float back = bounced + 6.f * wq(q) * cu;
-        if (!here) {
-          const double delta = wall_fraction(a, x, y, z, cx(q), cy(q), zs);
-          const float df = (float)delta;
-          px = (float)x - df * (float)cx(q);
-          py = (float)y - df * (float)cy(q);
-          cu = (float)cx(q) * (kda * (py - (float)a.y_ea - kh)) + (float)cy(q) * (kdh - kda * (px - (float)a.x_ea));
-          if (delta >= 0.5) {
-            back = (bounced + (2.f * df - 1.f) * a.fin[(size_t)q * a.n + idx] + 6.f * wq(q) * cu) / (2.f * df);
-          } else {
-            int xn = x + cx(q);
-            xn += xn < 0 ? a.nx : 0;
-            xn -= xn >= a.nx ? a.nx : 0;
-            int yn = y + cy(q);
-            yn += yn < 0 ? a.ny : 0;
-            yn -= yn >= a.ny ? a.ny : 0;
-            const int zn = z + cz(q);
-            const int zc = zn < 0 ? 0 : (zn > a.nz - 1 ? a.nz - 1 : zn);
-            const int nidx = (zc * a.ny + yn) * a.nx + xn;
-            if (zn == zc && !a.mask[nidx]) {
-              const float behind = a.fin[(size_t)o * a.n + nidx];
-              back = 2.f * df * bounced + (1.f - 2.f * df) * behind + 6.f * wq(q) * cu;
-            }
-          }
-          // momentum exchange relative to the fluid at rest
-          const float hit = bounced + back - 2.f * wq(q);
-          const float dfx = hit * (float)(-cx(q)), dfy = hit * (float)(-cy(q));
-          fx += dfx;
-          fy += dfy;
-          mz += (px - (float)a.x_ea) * dfy - (py - (float)a.y_ea - hz) * dfx;
-        }
+        if (!here) back = wetted_link(a, x, y, z, zs, idx, q, o, cx(q), cy(q), cz(q), wq(q), bounced, fx, fy, mz);
         val = back;
       }
       d[q] = val;
@@ -177,7 +192,7 @@ __global__ void __launch_bounds__(BX * BY) fsi_step_kernel(const __grid_constant
     feq_val<float, false>(rho_s, rho_s, usx, usy, usz, e1);
     const float keep = 1.f - sigma;
 #pragma unroll
-    for (int q = 0; q < Q; ++q) a.fout[(size_t)q * a.n + idx] = e1[q] + keep * (post[q] - e0[q]);
+    for (int q = 0; q < Q; ++q) __stcs(a.fout + (size_t)q * a.n + idx, e1[q] + keep * (post[q] - e0[q]));
     if (REPORT) {
       a.fld[0][idx] = mo.ux;
       a.fld[1][idx] = mo.uy;

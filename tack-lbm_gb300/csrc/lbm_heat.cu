@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(256) heat_kernel(const __grid_constant__ HeatA
       zs -= zs >= h.nz ? h.nz : 0;
       const int nidx = (zs * h.ny + ys) * h.nx + xs;
       src[q] = nidx;
-      const float pulled = h.g_in[(size_t)q * h.n + nidx];
+      const float pulled = load_l2(h.g_in + (size_t)q * h.n + nidx);
       float val = pulled;
       if (q != 0 && solid(h.geo, xs, ys, zs)) {
         const float bounced = h.g_in[(size_t)opp7(q) * h.n + idx];
@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(256) heat_kernel(const __grid_constant__ HeatA
     });
     float ux = 0.f, uy = 0.f, uz = 0.f, tau = h.tau0;
     if (!here) {
-      const float4 a = h.aux[idx];
+      const float4 a = __ldcs(h.aux + idx);  // read once, after the flow step wrote it
       ux = a.x;
       uy = a.y;
       uz = a.z;
@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(256) heat_kernel(const __grid_constant__ HeatA
       const float eq = w7(q) * temp * (1.f + 4.f * ((float)cx7(q) * ux + (float)cy7(q) * uy + (float)cz7(q) * uz));
       const float post = g[q] - om * (g[q] - eq);
       const float es = w7(q) * temp_s * (1.f + 4.f * ((float)cx7(q) * usx + (float)cy7(q) * usy + (float)cz7(q) * usz));
-      h.g_out[(size_t)q * h.n + idx] = es + keep * (post - eq);
+      __stcs(h.g_out + (size_t)q * h.n + idx, es + keep * (post - eq));
     });
     if (REPORT) {
       h.temp[idx] = here ? h.t_solid[idx] : temp;

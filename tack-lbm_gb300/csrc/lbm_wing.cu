@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(BX * BY) wing_step_kernel(const __grid_constan
       // source x - c_q
       const int src = idx + (cx(q) == 1 ? xm : cx(q) == -1 ? xp : 0) + (cy(q) == 1 ? ym : cy(q) == -1 ? yp : 0) +
                       (cz(q) == 1 ? zm : cz(q) == -1 ? zp : 0);
-      const float pulled = a.fin[(size_t)q * a.n + src];
+      const float pulled = load_l2(a.fin + (size_t)q * a.n + src);
       float val = pulled;
       if (q != 0 && a.mask[src]) {
         const float bounced = a.fin[(size_t)opp(q) * a.n + idx];
@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(BX * BY) wing_step_kernel(const __grid_constan
     feq_val<float, false>(rho_s, rho_s, usx, usy, usz, e1);
     const float keep = 1.f - sigma;
 #pragma unroll
-    for (int q = 0; q < Q; ++q) a.fout[(size_t)q * a.n + idx] = e1[q] + keep * (post[q] - e0[q]);
+    for (int q = 0; q < Q; ++q) __stcs(a.fout + (size_t)q * a.n + idx, e1[q] + keep * (post[q] - e0[q]));
     if (REPORT) {
       a.fld[0][idx] = mo.ux;
       a.fld[1][idx] = mo.uy;
