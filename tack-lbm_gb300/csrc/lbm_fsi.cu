@@ -139,11 +139,13 @@ __global__ void __launch_bounds__(BX * BY) fsi_step_kernel(const __grid_constant
   if (x < a.nx && y < a.ny) {
     const int idx = (z * a.ny + y) * a.nx + x;
     const bool here = a.mask[idx] != 0;
-    const float hz = a.kinf[z].x;
+    // every pulled value and every source's mask byte first (independent
+    // loads), then the links whose source is in the wing
     float d[Q];
+    uint32_t wall = 0;
     static_for<Q>([&](auto qc) {
       constexpr int q = decltype(qc)::value;
-      constexpr int o = opp(q);
+      constexpr int mq = dir(cx(q), cy(q), -cz(q));
       const int xr = x - cx(q);
       const int xs = xr < 0 ? 0 : (xr > a.nx - 1 ? a.nx - 1 : xr);
       int ys = y - cy(q);
@@ -152,28 +154,36 @@ __global__ void __launch_bounds__(BX * BY) fsi_step_kernel(const __grid_constant
       const int zr = z - cz(q);
       const bool flip = zr < 0 || zr > a.nz - 1;
       const int zs = zr < 0 ? 0 : (zr > a.nz - 1 ? a.nz - 1 : zr);
-      constexpr int mq = dir(cx(q), cy(q), -cz(q));
       const int src = (zs * a.ny + ys) * a.nx + xs;
-      float pulled;
       if (xr < 0) {
-        pulled = wq(q) * (1.f + 3.f * (float)cx(q) * a.u0 + 4.5f * (float)(cx(q) * cx(q)) * a.u0 * a.u0 -
-                          1.5f * a.u0 * a.u0);
+        d[q] = wq(q) * (1.f + 3.f * (float)cx(q) * a.u0 + 4.5f * (float)(cx(q) * cx(q)) * a.u0 * a.u0 -
+                        1.5f * a.u0 * a.u0);
       } else {
-        pulled = load_l2(a.fin + (size_t)(flip ? mq : q) * a.n + src);
+        d[q] = load_l2(a.fin + (size_t)(flip ? mq : q) * a.n + src);
       }
-      float val = pulled;
-      if (a.mask[src]) {
-        const float bounced = a.fin[(size_t)o * a.n + idx];
-        const float4 k = a.kinf[zs];
-        const float kh = k.x, kdh = k.y, kda = k.z;
-        float px = (float)x - 0.5f * (float)cx(q), py = (float)y - 0.5f * (float)cy(q);
-        float cu = (float)cx(q) * (kda * (py - (float)a.y_ea - kh)) + (float)cy(q) * (kdh - kda * (px - (float)a.x_ea));
-        float back = bounced + 6.f * wq(q) * cu;
-        if (!here) back = wetted_link(a, x, y, z, zs, idx, q, o, cx(q), cy(q), cz(q), wq(q), bounced, fx, fy, mz);
-        val = back;
-      }
-      d[q] = val;
+      // q = 0: a solid cell's own rest population bounces onto itself unchanged
+      if (q != 0 && a.mask[src]) wall |= 1u << q;
     });
+    if (wall) {
+      static_for<Q>([&](auto qc) {
+        constexpr int q = decltype(qc)::value;
+        constexpr int o = opp(q);
+        if (q != 0 && (wall >> q & 1u)) {
+          const int zr = z - cz(q);
+          const int zs = zr < 0 ? 0 : (zr > a.nz - 1 ? a.nz - 1 : zr);
+          const float bounced = a.fin[(size_t)o * a.n + idx];
+          if (here) {
+            const float4 k = a.kinf[zs];
+            const float px = (float)x - 0.5f * (float)cx(q), py = (float)y - 0.5f * (float)cy(q);
+            const float cu = (float)cx(q) * (k.z * (py - (float)a.y_ea - k.x)) +
+                             (float)cy(q) * (k.y - k.z * (px - (float)a.x_ea));
+            d[q] = bounced + 6.f * wq(q) * cu;
+          } else {
+            d[q] = wetted_link(a, x, y, z, zs, idx, q, o, cx(q), cy(q), cz(q), wq(q), bounced, fx, fy, mz);
+          }
+        }
+      });
+    }
     Pairs<float> pr;
     const Moments<float> mo = moments<float, false>(d, !here, pr);
     float post[Q];

@@ -71,35 +71,41 @@ __global__ void __launch_bounds__(BX * BY) wing_step_kernel(const __grid_constan
   if (x < a.nx && y < a.ny) {
     const int idx = (z * a.ny + y) * a.nx + x;
     const bool here = a.mask[idx] != 0;
-    const float fluid = here ? 0.f : 1.f;
     const int xm = x == 0 ? a.nx - 1 : -1, xp = x == a.nx - 1 ? 1 - a.nx : 1;
     const int ym = y == 0 ? (a.ny - 1) * a.nx : -a.nx, yp = y == a.ny - 1 ? -(a.ny - 1) * a.nx : a.nx;
     const int nxy = a.nx * a.ny;
     const int zm = z == 0 ? (a.nz - 1) * nxy : -nxy, zp = z == a.nz - 1 ? -(a.nz - 1) * nxy : nxy;
+    // every pulled value and every source's mask byte first (independent
+    // loads), then the links whose source is in the wing
     float d[Q];
+    uint32_t wall = 0;
     static_for<Q>([&](auto qc) {
       constexpr int q = decltype(qc)::value;
       // source x - c_q
       const int src = idx + (cx(q) == 1 ? xm : cx(q) == -1 ? xp : 0) + (cy(q) == 1 ? ym : cy(q) == -1 ? yp : 0) +
                       (cz(q) == 1 ? zm : cz(q) == -1 ? zp : 0);
-      const float pulled = load_l2(a.fin + (size_t)q * a.n + src);
-      float val = pulled;
-      if (q != 0 && a.mask[src]) {
-        const float bounced = a.fin[(size_t)opp(q) * a.n + idx];
-        const float px = (float)x - 0.5f * (float)cx(q), py = (float)y - 0.5f * (float)cy(q);
-        const float wx = a.da * (py - a.y_ea - a.h), wy = a.dh - a.da * (px - a.x_ea);
-        const float back = bounced + 6.f * wq(q) * ((float)cx(q) * wx + (float)cy(q) * wy);
-        val = back;
-        if (!here) {
-          const float hit = bounced + back;
-          const float dfx = hit * (float)(-cx(q)), dfy = hit * (float)(-cy(q));
-          fx += dfx;
-          fy += dfy;
-          mz += (px - a.x_ea) * dfy - (py - a.y_ea - a.h) * dfx;
-        }
-      }
-      d[q] = val;
+      d[q] = load_l2(a.fin + (size_t)q * a.n + src);
+      if (q != 0 && a.mask[src]) wall |= 1u << q;
     });
+    if (wall) {
+      static_for<Q>([&](auto qc) {
+        constexpr int q = decltype(qc)::value;
+        if (q != 0 && (wall >> q & 1u)) {
+          const float bounced = a.fin[(size_t)opp(q) * a.n + idx];
+          const float px = (float)x - 0.5f * (float)cx(q), py = (float)y - 0.5f * (float)cy(q);
+          const float wx = a.da * (py - a.y_ea - a.h), wy = a.dh - a.da * (px - a.x_ea);
+          const float back = bounced + 6.f * wq(q) * ((float)cx(q) * wx + (float)cy(q) * wy);
+          d[q] = back;
+          if (!here) {
+            const float hit = bounced + back;
+            const float dfx = hit * (float)(-cx(q)), dfy = hit * (float)(-cy(q));
+            fx += dfx;
+            fy += dfy;
+            mz += (px - a.x_ea) * dfy - (py - a.y_ea - a.h) * dfx;
+          }
+        }
+      });
+    }
     Pairs<float> pr;
     const Moments<float> mo = moments<float, false>(d, !here, pr);
     float post[Q];
