@@ -922,19 +922,23 @@ template <typename S, int COLL, bool REPORT, bool ODD>
 __device__ __forceinline__ void cell_step(const StepArgs<S> &a, int x0, int x, int y, int z) {
   using T = typename Store<S>::T;
   float v[NSUM] = {0, 0, 0, 0, 0, 0, 0, 0};
+  // a warp in the obstacle's reach box whose 32 link masks are all zero (no
+  // solid cell, no solid neighbour) takes the unmasked path; every lane
+  // votes, including those past the lattice's end (their mask words are 0)
+  const int ms = mask_slot(a, x0, y, z);
+  const uint32_t m = ms >= 0 ? a.masks[ms + (int)threadIdx.x] : 0u;
+  const bool walls = ms >= 0 && __any_sync(0xffffffffu, m != 0u);
   if (y < a.ny && !lid_row(a, y) && x < a.nx) {
     const int idx = (z * a.ny + y) * a.nx + x;
     const Row r = row_of(a, y, z);
-    const int ms = mask_slot(a, x0, y, z);
     const Offsets<S> o = cell_offsets(a, x, y, z);
     T d[Q];
     Prev prev{0.f, 0.f, 0.f, 0.f};
-    if (!(r.ylo || r.yhi || r.zlo || r.zhi) && ms < 0) {
+    if (!(r.ylo || r.yhi || r.zlo || r.zhi) && !walls) {
       if (REPORT) prev = load_prev(a.fld, idx);
       fast_load<S, ODD, false>(a, idx, o, r, 0u, d);
       fast_finish<S, COLL, REPORT, ODD, false>(a, x, y, idx, o, r, 0u, d, prev, v);
     } else {
-      const uint32_t m = ms >= 0 ? a.masks[ms + (int)threadIdx.x] : 0u;
       if (REPORT || !(m & MASK_SOLID)) {
         if (REPORT) prev = load_prev(a.fld, idx);
         fast_load<S, ODD, true>(a, idx, o, r, m, d);

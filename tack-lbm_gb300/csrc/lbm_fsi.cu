@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstring>
 #include <new>
 #include <string>
 #include <vector>
@@ -46,6 +47,7 @@ struct FsiArgs {
   float *fld[5];
   int nx, ny, nz, n;
   double chord, x_ea, y_ea, ea, span;
+  float x_eaf, y_eaf;  // the elastic axis in float32 for the per-cell arithmetic
   float u0, sponge_start, inv_sponge_len, sponge_strength;
   float omega_bgk, tau0, smag_c, magic;
 };
@@ -103,9 +105,9 @@ __device__ __noinline__ float wetted_link(const FsiArgs &a, int x, int y, int z,
   const double delta = wall_fraction(a, x, y, z, cxq, cyq, zs);
   const float df = (float)delta;
   const float px = (float)x - df * (float)cxq, py = (float)y - df * (float)cyq;
-  const float cu = (float)cxq * (kda * (py - (float)a.y_ea - kh)) + (float)cyq * (kdh - kda * (px - (float)a.x_ea));
-  float back = bounced + 6.f * w * ((float)cxq * (kda * ((float)y - 0.5f * (float)cyq - (float)a.y_ea - kh)) +
-                                    (float)cyq * (kdh - kda * ((float)x - 0.5f * (float)cxq - (float)a.x_ea)));
+  const float cu = (float)cxq * (kda * (py - a.y_eaf - kh)) + (float)cyq * (kdh - kda * (px - a.x_eaf));
+  float back = bounced + 6.f * w * ((float)cxq * (kda * ((float)y - 0.5f * (float)cyq - a.y_eaf - kh)) +
+                                    (float)cyq * (kdh - kda * ((float)x - 0.5f * (float)cxq - a.x_eaf)));
   if (delta >= 0.5) {
     back = (bounced + (2.f * df - 1.f) * a.fin[(size_t)q * a.n + idx] + 6.f * w * cu) / (2.f * df);
   } else {
@@ -128,41 +130,59 @@ __device__ __noinline__ float wetted_link(const FsiArgs &a, int x, int y, int z,
   const float dfx = hit * (float)(-cxq), dfy = hit * (float)(-cyq);
   fx += dfx;
   fy += dfy;
-  mz += (px - (float)a.x_ea) * dfy - (py - (float)a.y_ea - a.kinf[z].x) * dfx;
+  mz += (px - a.x_eaf) * dfy - (py - a.y_eaf - a.kinf[z].x) * dfx;
   return back;
+}
+
+// Can a cell of this block pull from a wing cell? The sections of layers
+// z-1..z+1 lie within `reach` of their elastic axes (lbm_naca.cuh), so a
+// block whose sources [x0-1, x0+32] x [y0-1, y0+4] miss those squares sees
+// no wing. Blocks on the periodic y edges are always checked cell by cell.
+__device__ __forceinline__ bool block_near_wing(const FsiArgs &a, int z) {
+  const int xb = (int)blockIdx.x * BX, yb = (int)blockIdx.y * BY;
+  if (yb == 0 || yb + BY >= a.ny) return true;
+  const float x0 = (float)(xb - 1), x1 = (float)(xb + BX), y0 = (float)(yb - 1), y1 = (float)(yb + BY);
+  const int z0 = z > 0 ? z - 1 : 0, z1 = z < a.nz - 1 ? z + 1 : a.nz - 1;
+  bool near = false;
+  for (int zz = z0; zz <= z1; ++zz) {
+    const NacaF &k = a.naca[zz];
+    near |= k.reach >= 0.f && x1 >= k.xc0 - k.reach && x0 <= k.xc0 + k.reach && y1 >= k.yc0 - k.reach &&
+            y0 <= k.yc0 + k.reach;
+  }
+  return near;
 }
 
 template <int COLL, bool REPORT>
 __global__ void __launch_bounds__(BX * BY) fsi_step_kernel(const __grid_constant__ FsiArgs a) {
   const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
+  const bool near = block_near_wing(a, z);
   float fx = 0.f, fy = 0.f, mz = 0.f;
   if (x < a.nx && y < a.ny) {
     const int idx = (z * a.ny + y) * a.nx + x;
-    const bool here = a.mask[idx] != 0;
-    // every pulled value and every source's mask byte first (independent
-    // loads), then the links whose source is in the wing
+    const bool here = near && a.mask[idx] != 0;
+    // source offsets: inflow at x = 0 (no source), zero-gradient outflow at
+    // x = nx - 1, periodic y, mirror planes below z = 0 and above z = nz - 1
+    const bool inflow = x == 0;
+    const int xm = inflow ? 0 : -1, xp = x == a.nx - 1 ? 0 : 1;
+    const int ym = y == 0 ? (a.ny - 1) * a.nx : -a.nx, yp = y == a.ny - 1 ? -(a.ny - 1) * a.nx : a.nx;
+    const int nxy = a.nx * a.ny;
+    const bool zlo = z == 0, zhi = z == a.nz - 1;
+    const int zm = zlo ? 0 : -nxy, zp = zhi ? 0 : nxy;
+    // every pulled value and, near the wing, every source's mask byte first
+    // (independent loads), then the links whose source is in the wing
     float d[Q];
     uint32_t wall = 0;
     static_for<Q>([&](auto qc) {
       constexpr int q = decltype(qc)::value;
       constexpr int mq = dir(cx(q), cy(q), -cz(q));
-      const int xr = x - cx(q);
-      const int xs = xr < 0 ? 0 : (xr > a.nx - 1 ? a.nx - 1 : xr);
-      int ys = y - cy(q);
-      ys += ys < 0 ? a.ny : 0;
-      ys -= ys >= a.ny ? a.ny : 0;
-      const int zr = z - cz(q);
-      const bool flip = zr < 0 || zr > a.nz - 1;
-      const int zs = zr < 0 ? 0 : (zr > a.nz - 1 ? a.nz - 1 : zr);
-      const int src = (zs * a.ny + ys) * a.nx + xs;
-      if (xr < 0) {
-        d[q] = wq(q) * (1.f + 3.f * (float)cx(q) * a.u0 + 4.5f * (float)(cx(q) * cx(q)) * a.u0 * a.u0 -
-                        1.5f * a.u0 * a.u0);
-      } else {
-        d[q] = load_l2(a.fin + (size_t)(flip ? mq : q) * a.n + src);
-      }
+      const int src = idx + (cx(q) == 1 ? xm : cx(q) == -1 ? xp : 0) + (cy(q) == 1 ? ym : cy(q) == -1 ? yp : 0) +
+                      (cz(q) == 1 ? zm : cz(q) == -1 ? zp : 0);
+      const bool flip = (cz(q) == 1 && zlo) || (cz(q) == -1 && zhi);
+      d[q] = load_l2(a.fin + (size_t)(flip ? mq : q) * a.n + src);
+      if (cx(q) == 1 && inflow)
+        d[q] = wq(q) * (1.f + 3.f * a.u0 + 4.5f * a.u0 * a.u0 - 1.5f * a.u0 * a.u0);
       // q = 0: a solid cell's own rest population bounces onto itself unchanged
-      if (q != 0 && a.mask[src]) wall |= 1u << q;
+      if (q != 0 && near && a.mask[src]) wall |= 1u << q;
     });
     if (wall) {
       static_for<Q>([&](auto qc) {
@@ -175,8 +195,7 @@ __global__ void __launch_bounds__(BX * BY) fsi_step_kernel(const __grid_constant
           if (here) {
             const float4 k = a.kinf[zs];
             const float px = (float)x - 0.5f * (float)cx(q), py = (float)y - 0.5f * (float)cy(q);
-            const float cu = (float)cx(q) * (k.z * (py - (float)a.y_ea - k.x)) +
-                             (float)cy(q) * (k.y - k.z * (px - (float)a.x_ea));
+            const float cu = (float)cx(q) * (k.z * (py - a.y_eaf - k.x)) + (float)cy(q) * (k.y - k.z * (px - a.x_eaf));
             d[q] = bounced + 6.f * wq(q) * cu;
           } else {
             d[q] = wetted_link(a, x, y, z, zs, idx, q, o, cx(q), cy(q), cz(q), wq(q), bounced, fx, fy, mz);
@@ -193,8 +212,8 @@ __global__ void __launch_bounds__(BX * BY) fsi_step_kernel(const __grid_constant
     const float t = fmaxf(0.f, ((float)x - a.sponge_start) * a.inv_sponge_len);
     const float sigma = here ? 1.f : a.sponge_strength * t * t;
     const float4 k = a.kinf[z];
-    const float wx = k.z * ((float)y - (float)a.y_ea - k.x);
-    const float wy = k.y - k.z * ((float)x - (float)a.x_ea);
+    const float wx = k.z * ((float)y - a.y_eaf - k.x);
+    const float wy = k.y - k.z * ((float)x - a.x_eaf);
     const float rho_s = mo.rho + sigma * (1.f - mo.rho);
     const float usx = here ? wx : mo.ux, usy = here ? wy : mo.uy, usz = here ? 0.f : mo.uz;
     float e0[Q], e1[Q];
@@ -211,20 +230,18 @@ __global__ void __launch_bounds__(BX * BY) fsi_step_kernel(const __grid_constant
       a.fld[4][idx] = sqrtf(mo.ux * mo.ux + mo.uy * mo.uy + mo.uz * mo.uz);
     }
   }
-  __shared__ float red[BY][3];
-  float v[3] = {fx, fy, mz};
+  // the layer's loads: warp sums, one float64 atomic per warp and component
+  // where the warp touched the wing (no block barrier)
+  if (near) {
+    float v[3] = {fx, fy, mz};
 #pragma unroll
-  for (int c = 0; c < 3; ++c) {
+    for (int c = 0; c < 3; ++c) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v[c] += __shfl_down_sync(0xffffffffu, v[c], o);
-  }
-  if (threadIdx.x == 0)
-    for (int c = 0; c < 3; ++c) red[threadIdx.y][c] = v[c];
-  __syncthreads();
-  if (threadIdx.y == 0 && threadIdx.x < 3) {
-    float s = 0.f;
-    for (int w = 0; w < BY; ++w) s += red[w][threadIdx.x];
-    if (s != 0.f) atomicAdd(&a.load[3 * z + threadIdx.x], (double)s);
+      for (int o = 16; o > 0; o >>= 1) v[c] += __shfl_down_sync(0xffffffffu, v[c], o);
+    }
+    if (threadIdx.x == 0)
+      for (int c = 0; c < 3; ++c)
+        if (v[c] != 0.f) atomicAdd(&a.load[3 * z + c], (double)v[c]);
   }
 }
 
@@ -257,6 +274,8 @@ struct lbm_fsi {
   uint8_t *mask = nullptr;
   double *kin = nullptr;  // one buffer: KIN doubles, a float4 and a NacaF per layer
   double *load = nullptr;
+  unsigned char *kin_host = nullptr;  // pinned staging of kin (uploaded stream-ordered)
+  double *load_host = nullptr;        // pinned staging of the loads
   float *fld[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   int stride = 1;
   int out_dims[3] = {0, 0, 0};
@@ -297,6 +316,8 @@ void frelease(lbm_fsi *w) {
   cudaFree(w->mask);
   cudaFree(w->kin);
   cudaFree(w->load);
+  cudaFreeHost(w->kin_host);
+  cudaFreeHost(w->load_host);
   for (int k = 0; k < 5; ++k) {
     if (w->stride > 1) cudaFree(w->out[k]);
     cudaFree(w->fld[k]);
@@ -322,6 +343,8 @@ lbmf::FsiArgs fargs(const lbm_fsi *w) {
   a.y_ea = c.y_ea;
   a.ea = c.ea;
   a.span = c.span;
+  a.x_eaf = (float)c.x_ea;
+  a.y_eaf = (float)c.y_ea;
   a.u0 = (float)c.u0;
   a.sponge_start = (float)c.sponge_start;
   a.inv_sponge_len = (float)(1.0 / ((double)c.nx - c.sponge_start));
@@ -340,8 +363,9 @@ size_t kin_bytes(int nz) { return (size_t)nz * (lbmf::KIN * sizeof(double) + siz
 lbm_status set_kin(lbm_fsi *w, const double *kin) {
   const lbm_fsi_config &c = w->cfg;
   const int nz = c.nz;
-  std::vector<unsigned char> buf(kin_bytes(nz));
-  double *k = reinterpret_cast<double *>(buf.data());
+  // the previous upload from the staging buffer has finished once the stream is idle
+  FCUDA(cudaStreamSynchronize(0));
+  double *k = reinterpret_cast<double *>(w->kin_host);
   float4 *kf = reinterpret_cast<float4 *>(k + lbmf::KIN * nz);
   lbmk::NacaF *nf = reinterpret_cast<lbmk::NacaF *>(kf + nz);
   for (int z = 0; z < nz; ++z) {
@@ -353,7 +377,7 @@ lbm_status set_kin(lbm_fsi *w, const double *kin) {
                               k[lbmf::KIN * z + 5]);
     if (!((double)z + 0.5 < c.span)) nf[z].reach = -1.f;  // past the tip: no section
   }
-  FCUDA(cudaMemcpy(w->kin, buf.data(), buf.size(), cudaMemcpyHostToDevice));
+  FCUDA(cudaMemcpyAsync(w->kin, w->kin_host, kin_bytes(nz), cudaMemcpyHostToDevice, 0));
   lbmf::fsi_mask_kernel<<<lbmk::cell_grid(w->n), 256>>>(fargs(w), w->mask);
   FCUDA(cudaGetLastError());
   return LBM_OK;
@@ -399,6 +423,8 @@ lbm_status lbm_fsi_create(const lbm_fsi_config *cfg, lbm_fsi **out) {
   if (e == cudaSuccess) e = cudaMalloc(&w->f[1], fb);
   if (e == cudaSuccess) e = cudaMalloc(&w->mask, (size_t)w->n);
   if (e == cudaSuccess) e = cudaMalloc(&w->kin, kin_bytes(cfg->nz));
+  if (e == cudaSuccess) e = cudaMallocHost(&w->kin_host, kin_bytes(cfg->nz));
+  if (e == cudaSuccess) e = cudaMallocHost(&w->load_host, (size_t)3 * cfg->nz * sizeof(double));
   if (e == cudaSuccess) e = cudaMemset(w->kin, 0, kin_bytes(cfg->nz));
   if (e == cudaSuccess) e = cudaMalloc(&w->load, (size_t)3 * cfg->nz * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&w->ptrs, 10 * sizeof(float *));
@@ -452,7 +478,10 @@ lbm_status lbm_fsi_step(lbm_fsi *w, int32_t report, const double *kin, double *l
     default: launch_fsi<lbmk::COLL_LES>(w, a, report != 0); break;
   }
   FCUDA(cudaGetLastError());
-  FCUDA(cudaMemcpy(load, w->load, (size_t)3 * w->cfg.nz * sizeof(double), cudaMemcpyDeviceToHost));
+  const size_t lb = (size_t)3 * w->cfg.nz * sizeof(double);
+  FCUDA(cudaMemcpyAsync(w->load_host, w->load, lb, cudaMemcpyDeviceToHost, 0));
+  FCUDA(cudaStreamSynchronize(0));
+  std::memcpy(load, w->load_host, lb);
   w->cur ^= 1;
   return LBM_OK;
 }
