@@ -211,17 +211,24 @@ __global__ void __launch_bounds__(BX * BY) fsi_step_kernel(const __grid_constant
     collide<float, COLL, false>(post, mo, pr, a.omega_bgk, a.tau0, a.smag_c, a.magic);
     const float t = fmaxf(0.f, ((float)x - a.sponge_start) * a.inv_sponge_len);
     const float sigma = here ? 1.f : a.sponge_strength * t * t;
-    const float4 k = a.kinf[z];
-    const float wx = k.z * ((float)y - a.y_eaf - k.x);
-    const float wy = k.y - k.z * ((float)x - a.x_eaf);
-    const float rho_s = mo.rho + sigma * (1.f - mo.rho);
-    const float usx = here ? wx : mo.ux, usy = here ? wy : mo.uy, usz = here ? 0.f : mo.uz;
-    float e0[Q], e1[Q];
-    feq_val<float, false>(mo.rho, mo.rho, mo.ux, mo.uy, mo.uz, e0);
-    feq_val<float, false>(rho_s, rho_s, usx, usy, usz, e1);
-    const float keep = 1.f - sigma;
+    // the sponge blend feq(rho_s, u_s) + (1 - sigma)(post - feq(rho, u)); at
+    // sigma = 0 it is post up to one rounding, so the cells before the
+    // sponge skip it
+    if (sigma != 0.f) {
+      const float4 k = a.kinf[z];
+      const float wx = k.z * ((float)y - a.y_eaf - k.x);
+      const float wy = k.y - k.z * ((float)x - a.x_eaf);
+      const float rho_s = mo.rho + sigma * (1.f - mo.rho);
+      const float usx = here ? wx : mo.ux, usy = here ? wy : mo.uy, usz = here ? 0.f : mo.uz;
+      float e0[Q], e1[Q];
+      feq_val<float, false>(mo.rho, mo.rho, mo.ux, mo.uy, mo.uz, e0);
+      feq_val<float, false>(rho_s, rho_s, usx, usy, usz, e1);
+      const float keep = 1.f - sigma;
 #pragma unroll
-    for (int q = 0; q < Q; ++q) __stcs(a.fout + (size_t)q * a.n + idx, e1[q] + keep * (post[q] - e0[q]));
+      for (int q = 0; q < Q; ++q) post[q] = e1[q] + keep * (post[q] - e0[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q) __stcs(a.fout + (size_t)q * a.n + idx, post[q]);
     if (REPORT) {
       a.fld[0][idx] = mo.ux;
       a.fld[1][idx] = mo.uy;

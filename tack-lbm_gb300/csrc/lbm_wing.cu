@@ -114,16 +114,22 @@ __global__ void __launch_bounds__(BX * BY) wing_step_kernel(const __grid_constan
     collide<float, COLL, false>(post, mo, pr, a.omega_bgk, a.tau0, a.smag_c, a.magic);
     const float t = fmaxf(0.f, ((float)x - a.sponge_start) * a.inv_sponge_len);
     const float sigma = here ? 1.f : a.sponge_strength * t * t;
-    const float wx = a.da * ((float)y - a.y_ea - a.h), wy = a.dh - a.da * ((float)x - a.x_ea);
-    const float tx = here ? wx : a.u0, ty = here ? wy : 0.f;
-    const float rho_s = mo.rho + sigma * (1.f - mo.rho);
-    const float usx = mo.ux + sigma * (tx - mo.ux), usy = mo.uy + sigma * (ty - mo.uy), usz = (1.f - sigma) * mo.uz;
-    float e0[Q], e1[Q];
-    feq_val<float, false>(mo.rho, mo.rho, mo.ux, mo.uy, mo.uz, e0);
-    feq_val<float, false>(rho_s, rho_s, usx, usy, usz, e1);
-    const float keep = 1.f - sigma;
+    // the sponge blend; at sigma = 0 it is post up to one rounding
+    if (sigma != 0.f) {
+      const float wx = a.da * ((float)y - a.y_ea - a.h), wy = a.dh - a.da * ((float)x - a.x_ea);
+      const float tx = here ? wx : a.u0, ty = here ? wy : 0.f;
+      const float rho_s = mo.rho + sigma * (1.f - mo.rho);
+      const float usx = mo.ux + sigma * (tx - mo.ux), usy = mo.uy + sigma * (ty - mo.uy),
+                  usz = (1.f - sigma) * mo.uz;
+      float e0[Q], e1[Q];
+      feq_val<float, false>(mo.rho, mo.rho, mo.ux, mo.uy, mo.uz, e0);
+      feq_val<float, false>(rho_s, rho_s, usx, usy, usz, e1);
+      const float keep = 1.f - sigma;
 #pragma unroll
-    for (int q = 0; q < Q; ++q) __stcs(a.fout + (size_t)q * a.n + idx, e1[q] + keep * (post[q] - e0[q]));
+      for (int q = 0; q < Q; ++q) post[q] = e1[q] + keep * (post[q] - e0[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q) __stcs(a.fout + (size_t)q * a.n + idx, post[q]);
     if (REPORT) {
       a.fld[0][idx] = mo.ux;
       a.fld[1][idx] = mo.uy;
