@@ -63,31 +63,32 @@ __device__ __forceinline__ bool section64(const FsiArgs &a, double x, double y, 
   return xc >= 0.0 && xc <= 1.0 && fabs(t) < half && (double)z + 0.5 < a.span;
 }
 
-// the section test at (xf, yf) = (x, y) exactly representable in float32
-__device__ __forceinline__ bool section(const FsiArgs &a, float xf, float yf, double x, double y, int z) {
-  const int r = naca_prefilter(a.naca[z], xf, yf);
-  return r != 0 ? r > 0 : section64(a, x, y, z);
+// the section test at (x, y), both exactly representable in float32 (lattice
+// points, and the k/64 points of the wall bisection)
+__device__ __forceinline__ bool section(const FsiArgs &a, float x, float y, int z) {
+  const int r = naca_prefilter(a.naca[z], x, y);
+  return r != 0 ? r > 0 : section64(a, (double)x, (double)y, z);
 }
 
 __global__ void fsi_mask_kernel(const __grid_constant__ FsiArgs a, uint8_t *mask) {
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < a.n; idx += gridDim.x * blockDim.x) {
     const int x = idx % a.nx, y = (idx / a.nx) % a.ny, z = idx / (a.nx * a.ny);
-    mask[idx] = section(a, (float)x, (float)y, (double)x, (double)y, z) ? 1 : 0;
+    mask[idx] = section(a, (float)x, (float)y, z) ? 1 : 0;
   }
 }
 
 // the wall's place on the link from (x, y, z) toward (x - cx, y - cy, zs), as a fraction
-__device__ __forceinline__ double wall_fraction(const FsiArgs &a, int x, int y, int z, int cxq, int cyq, int zs) {
-  double lo = 0.0, hi = 1.0;
+// (the bisection's points k/64 and the points x - mid c_q are exact in
+// float32, so float32 carries it with the float64 results of the test)
+__device__ __forceinline__ float wall_fraction(const FsiArgs &a, int x, int y, int z, int cxq, int cyq, int zs) {
+  float lo = 0.f, hi = 1.f;
   for (int it = 0; it < 6; ++it) {
-    const double mid = 0.5 * (lo + hi);  // k / 64: the offsets below are exact in float32
-    const float mf = (float)mid;
-    const bool in = section(a, (float)x - mf * (float)cxq, (float)y - mf * (float)cyq, (double)x - mid * cxq,
-                            (double)y - mid * cyq, mid >= 0.5 ? zs : z);
+    const float mid = 0.5f * (lo + hi);
+    const bool in = section(a, (float)x - mid * (float)cxq, (float)y - mid * (float)cyq, mid >= 0.5f ? zs : z);
     if (in) hi = mid;
     else lo = mid;
   }
-  return 0.5 * (lo + hi);
+  return 0.5f * (lo + hi);
 }
 
 // The interpolated bounce-back of one wetted link, a fluid cell (x, y, z)
@@ -102,13 +103,12 @@ __device__ __noinline__ float wetted_link(const FsiArgs &a, int x, int y, int z,
                                           float &mz) {
   const float4 k = a.kinf[zs];
   const float kh = k.x, kdh = k.y, kda = k.z;
-  const double delta = wall_fraction(a, x, y, z, cxq, cyq, zs);
-  const float df = (float)delta;
+  const float df = wall_fraction(a, x, y, z, cxq, cyq, zs);
   const float px = (float)x - df * (float)cxq, py = (float)y - df * (float)cyq;
   const float cu = (float)cxq * (kda * (py - a.y_eaf - kh)) + (float)cyq * (kdh - kda * (px - a.x_eaf));
   float back = bounced + 6.f * w * ((float)cxq * (kda * ((float)y - 0.5f * (float)cyq - a.y_eaf - kh)) +
                                     (float)cyq * (kdh - kda * ((float)x - 0.5f * (float)cxq - a.x_eaf)));
-  if (delta >= 0.5) {
+  if (df >= 0.5f) {
     back = (bounced + (2.f * df - 1.f) * a.fin[(size_t)q * a.n + idx] + 6.f * w * cu) / (2.f * df);
   } else {
     int xn = x + cxq;

@@ -42,70 +42,95 @@ struct HeatArgs {
   int nx, ny, nz, n;
   float u0, sponge_start, inv_sponge_len, sponge_strength;
   float alpha, nu, tau0;
+  // the flow step's link masks (bit q, q = 1..6: the source x - c_q is solid;
+  // bit 19: the cell is solid) over the obstacle's reach box; used when y and
+  // z are periodic, where the flow's sources are the temperature's sources
+  const uint32_t *masks;
+  int reach_lo[3], reach_hi[3], reach_any, use_masks;
 };
 
+// first link-mask word of the 32-cell row segment at x0, or -1 outside the reach box
+__device__ __forceinline__ int heat_mask_slot(const HeatArgs &h, int x0, int y, int z) {
+  if (!h.reach_any || x0 + BX - 1 < h.reach_lo[0] || x0 > h.reach_hi[0] || y < h.reach_lo[1] ||
+      y > h.reach_hi[1] || z < h.reach_lo[2] || z > h.reach_hi[2])
+    return -1;
+  const int w0 = h.reach_lo[0] / BX, nw = h.reach_hi[0] / BX - w0 + 1;
+  const int nyr = h.reach_hi[1] - h.reach_lo[1] + 1;
+  return (((z - h.reach_lo[2]) * nyr + (y - h.reach_lo[1])) * nw + (x0 / BX - w0)) * BX;
+}
+
+// One cell per thread; a warp is a 32-cell row segment (block 32 x 8).
 template <bool REPORT>
 __global__ void __launch_bounds__(256) heat_kernel(const __grid_constant__ HeatArgs h) {
-  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < h.n; idx += gridDim.x * blockDim.x) {
-    const int x = idx % h.nx, y = (idx / h.nx) % h.ny, z = idx / (h.nx * h.ny);
-    const bool here = solid(h.geo, x, y, z);
-    const float fluid = here ? 0.f : 1.f;
-    float g[7], temp = 0.f;
-    int src[7];
-    static_for<7>([&](auto qc) {
-      constexpr int q = decltype(qc)::value;
-      int xs = x - cx7(q), ys = y - cy7(q), zs = z - cz7(q);
-      xs += xs < 0 ? h.nx : 0;
-      xs -= xs >= h.nx ? h.nx : 0;
-      ys += ys < 0 ? h.ny : 0;
-      ys -= ys >= h.ny ? h.ny : 0;
-      zs += zs < 0 ? h.nz : 0;
-      zs -= zs >= h.nz ? h.nz : 0;
-      const int nidx = (zs * h.ny + ys) * h.nx + xs;
-      src[q] = nidx;
-      const float pulled = load_l2(h.g_in + (size_t)q * h.n + nidx);
-      float val = pulled;
-      if (q != 0 && solid(h.geo, xs, ys, zs)) {
-        const float bounced = h.g_in[(size_t)opp7(q) * h.n + idx];
-        val = sink(h.geo, xs, ys, zs) ? -bounced + 2.0f * w7(q) * h.t_solid[nidx] : bounced;
-      }
-      g[q] = val;
-      temp += val;
-    });
-    float ux = 0.f, uy = 0.f, uz = 0.f, tau = h.tau0;
-    if (!here) {
-      const float4 a = __ldcs(h.aux + idx);  // read once, after the flow step wrote it
-      ux = a.x;
-      uy = a.y;
-      uz = a.z;
-      tau = a.w;
+  const int x0 = (int)blockIdx.x * BX, x = x0 + (int)threadIdx.x;
+  const int y = (int)blockIdx.y * blockDim.y + (int)threadIdx.y, z = (int)blockIdx.z;
+  if (y >= h.ny) return;  // whole warps: blockDim.x is 32
+  uint32_t m = 0;
+  if (h.use_masks) {
+    const int ms = heat_mask_slot(h, x0, y, z);
+    m = ms >= 0 ? h.masks[ms + (int)threadIdx.x] : 0u;
+  }
+  if (x >= h.nx) return;
+  const int idx = (z * h.ny + y) * h.nx + x;
+  const bool here = h.use_masks ? (m & MASK_SOLID) != 0 : solid(h.geo, x, y, z);
+  const float fluid = here ? 0.f : 1.f;
+  float g[7], temp = 0.f;
+  int src[7];
+  static_for<7>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    int xs = x - cx7(q), ys = y - cy7(q), zs = z - cz7(q);
+    xs += xs < 0 ? h.nx : 0;
+    xs -= xs >= h.nx ? h.nx : 0;
+    ys += ys < 0 ? h.ny : 0;
+    ys -= ys >= h.ny ? h.ny : 0;
+    zs += zs < 0 ? h.nz : 0;
+    zs -= zs >= h.nz ? h.nz : 0;
+    const int nidx = (zs * h.ny + ys) * h.nx + xs;
+    src[q] = nidx;
+    const float pulled = load_l2(h.g_in + (size_t)q * h.n + nidx);
+    float val = pulled;
+    // D3Q7 direction q (1..6) is D3Q19 direction q: the same link-mask bit
+    const bool wall = q != 0 && (h.use_masks ? ((m >> q) & 1u) != 0 : solid(h.geo, xs, ys, zs));
+    if (wall) {
+      const float bounced = h.g_in[(size_t)opp7(q) * h.n + idx];
+      val = sink(h.geo, xs, ys, zs) ? -bounced + 2.0f * w7(q) * h.t_solid[nidx] : bounced;
     }
-    const float t = fmaxf(0.f, ((float)x - h.sponge_start) * h.inv_sponge_len);
-    const float sigma = here ? 1.f : h.sponge_strength * t * t;
-    const float keep = 1.f - sigma;
-    const float usx = ux + sigma * (h.u0 * fluid - ux), usy = keep * uy, usz = keep * uz;
-    const float alpha = h.alpha + fmaxf(0.f, (tau - 0.5f) * (1.f / 3.f) - h.nu) * (1.f / PR_T);
-    const float om = 1.f / (4.f * alpha + 0.5f);
-    const float temp_s = keep * temp;
-    static_for<7>([&](auto qc) {
-      constexpr int q = decltype(qc)::value;
-      const float eq = w7(q) * temp * (1.f + 4.f * ((float)cx7(q) * ux + (float)cy7(q) * uy + (float)cz7(q) * uz));
-      const float post = g[q] - om * (g[q] - eq);
-      const float es = w7(q) * temp_s * (1.f + 4.f * ((float)cx7(q) * usx + (float)cy7(q) * usy + (float)cz7(q) * usz));
-      __stcs(h.g_out + (size_t)q * h.n + idx, es + keep * (post - eq));
-    });
-    if (REPORT) {
-      h.temp[idx] = here ? h.t_solid[idx] : temp;
-      if (!here) {
-        static_for<7>([&](auto qc) {
-          constexpr int q = decltype(qc)::value;
-          if (q != 0) {
-            const int s = src[q];
-            const int xs = s % h.nx, ys = (s / h.nx) % h.ny, zs = s / (h.nx * h.ny);
-            if (sink(h.geo, xs, ys, zs)) atomicAdd(&h.q_solid[s], temp);
-          }
-        });
-      }
+    g[q] = val;
+    temp += val;
+  });
+  float ux = 0.f, uy = 0.f, uz = 0.f, tau = h.tau0;
+  if (!here) {
+    const float4 a = __ldcs(h.aux + idx);  // read once, after the flow step wrote it
+    ux = a.x;
+    uy = a.y;
+    uz = a.z;
+    tau = a.w;
+  }
+  const float t = fmaxf(0.f, ((float)x - h.sponge_start) * h.inv_sponge_len);
+  const float sigma = here ? 1.f : h.sponge_strength * t * t;
+  const float keep = 1.f - sigma;
+  const float usx = ux + sigma * (h.u0 * fluid - ux), usy = keep * uy, usz = keep * uz;
+  const float alpha = h.alpha + fmaxf(0.f, (tau - 0.5f) * (1.f / 3.f) - h.nu) * (1.f / PR_T);
+  const float om = 1.f / (4.f * alpha + 0.5f);
+  const float temp_s = keep * temp;
+  static_for<7>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    const float eq = w7(q) * temp * (1.f + 4.f * ((float)cx7(q) * ux + (float)cy7(q) * uy + (float)cz7(q) * uz));
+    const float post = g[q] - om * (g[q] - eq);
+    const float es = w7(q) * temp_s * (1.f + 4.f * ((float)cx7(q) * usx + (float)cy7(q) * usy + (float)cz7(q) * usz));
+    __stcs(h.g_out + (size_t)q * h.n + idx, es + keep * (post - eq));
+  });
+  if (REPORT) {
+    h.temp[idx] = here ? h.t_solid[idx] : temp;
+    if (!here) {
+      static_for<7>([&](auto qc) {
+        constexpr int q = decltype(qc)::value;
+        if (q != 0) {
+          const int s = src[q];
+          const int xs = s % h.nx, ys = (s / h.nx) % h.ny, zs = s / (h.nx * h.ny);
+          if (sink(h.geo, xs, ys, zs)) atomicAdd(&h.q_solid[s], temp);
+        }
+      });
     }
   }
 }
@@ -135,12 +160,20 @@ cudaError_t launch_heat(const Ctx &c, bool report, cudaStream_t st) {
   h.alpha = (float)g.alpha;
   h.nu = (float)g.heat_nu;
   h.tau0 = (float)(3.0 * g.nu + 0.5);
-  const int grid = lbmk::cell_grid(c.n);
+  h.masks = c.wmasks;
+  for (int k = 0; k < 3; ++k) {
+    h.reach_lo[k] = c.reach_lo[k];
+    h.reach_hi[k] = c.reach_hi[k];
+  }
+  h.reach_any = c.reach_any;
+  h.use_masks = g.lateral == LBM_PERIODIC && g.vertical == LBM_PERIODIC && (!c.reach_any || c.wmasks) ? 1 : 0;
+  const dim3 block(lbmk::BX, 8);
+  const dim3 grid((g.nx + lbmk::BX - 1) / lbmk::BX, (g.ny + 7) / 8, g.nz);
   if (report) {
     cudaMemsetAsync(c.heat_fld[LBM_Q_SOLID], 0, (size_t)c.n * sizeof(float), st);
-    lbmk::heat_kernel<true><<<grid, 256, 0, st>>>(h);
+    lbmk::heat_kernel<true><<<grid, block, 0, st>>>(h);
   } else {
-    lbmk::heat_kernel<false><<<grid, 256, 0, st>>>(h);
+    lbmk::heat_kernel<false><<<grid, block, 0, st>>>(h);
   }
   return cudaGetLastError();
 }
