@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(BX * BY) fsi_step_kernel(const __grid_constant
     }
     if (threadIdx.x == 0)
       for (int c = 0; c < 3; ++c)
-        if (v[c] != 0.f) atomicAdd(&a.load[3 * z + c], float_to_double_int(v[c]));
+        if (v[c] != 0.f) atomicAdd(&a.load[3 * z + c], (double)v[c]);
   }
 }
 

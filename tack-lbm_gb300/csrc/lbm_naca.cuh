@@ -42,19 +42,6 @@ __device__ __forceinline__ int naca_prefilter(const NacaF &k, float x, float y) 
   return gap < -k.margin ? 1 : (gap > k.margin ? -1 : 0);
 }
 
-// float -> double by integer operations, for the float64 load atomics: the
-// conversion instruction runs on the float64 pipe, which issues slowly on
-// GB300. Exact for normal numbers, infinities and NaN; subnormals (below
-// 1.2e-38 in magnitude) become zero of the same sign.
-__device__ __forceinline__ double float_to_double_int(float f) {
-  const uint32_t u = __float_as_uint(f);
-  const uint32_t e = (u >> 23) & 0xffu;
-  const uint64_t sign = (uint64_t)(u & 0x80000000u) << 32;
-  if (e == 0u) return __longlong_as_double((long long)sign);
-  const uint64_t e64 = e == 0xffu ? 0x7ffull : (uint64_t)(e + 896u);  // 1023 - 127
-  return __longlong_as_double((long long)(sign | (e64 << 52) | ((uint64_t)(u & 0x7fffffu) << 29)));
-}
-
 inline NacaF make_naca_f(double chord, double x_ea, double yc, double ea, double ca, double sa) {
   NacaF k;
   k.xc0 = (float)x_ea;

@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(BX * BY) wing_step_kernel(const __grid_constan
   if (threadIdx.y == 0 && threadIdx.x < 3) {
     float s = 0.f;
     for (int w = 0; w < BY; ++w) s += red[w][threadIdx.x];
-    if (s != 0.f) atomicAdd(&a.load[threadIdx.x], float_to_double_int(s));
+    if (s != 0.f) atomicAdd(&a.load[threadIdx.x], (double)s);
   }
 }
 
