@@ -913,9 +913,20 @@ __device__ __forceinline__ bool lid_row(const StepArgs<S> &a, int y) {
   return a.lateral == SIDE_LID && y == a.ny - 1;
 }
 
+// Resident step_kernel blocks per SM, by storage width. FP32 stays at 5
+// blocks (20 warps, no spills; 24 warps measured no faster). FP16/BF16 are
+// latency-bound with half the bytes in flight per warp: 8 blocks (32 warps,
+// 64 registers) run 7 % faster despite ~120 bytes of spills to L1.
 #ifndef LBM_STEP_MIN_BLOCKS
 #define LBM_STEP_MIN_BLOCKS 5
 #endif
+#ifndef LBM_STEP_MIN_BLOCKS_16
+#define LBM_STEP_MIN_BLOCKS_16 8
+#endif
+template <typename S>
+__host__ __device__ constexpr int step_min_blocks() {
+  return sizeof(S) == 2 ? LBM_STEP_MIN_BLOCKS_16 : LBM_STEP_MIN_BLOCKS;
+}
 
 // One cell of the per-cell kernels: the warp is the 32-cell row segment at x0.
 template <typename S, int COLL, bool REPORT, bool ODD>
@@ -956,7 +967,7 @@ __host__ __device__ constexpr int tile_warps_x() {
 }
 
 template <typename S, int COLL, bool REPORT, bool ODD>
-__global__ void __launch_bounds__(BX * BY, LBM_STEP_MIN_BLOCKS)
+__global__ void __launch_bounds__(BX * BY, step_min_blocks<S>())
 step_kernel(const __grid_constant__ StepArgs<S> a) {
   constexpr int TX = tile_warps_x<S>(), TY = BY / TX;
   const int wx = (int)threadIdx.y % TX, wy = (int)threadIdx.y / TX;
