@@ -915,13 +915,13 @@ __device__ __forceinline__ bool lid_row(const StepArgs<S> &a, int y) {
 
 // Resident step_kernel blocks per SM, by storage width. FP32 stays at 5
 // blocks (20 warps, no spills; 24 warps measured no faster). FP16/BF16 are
-// latency-bound with half the bytes in flight per warp: 8 blocks (32 warps,
-// 64 registers) run 7 % faster despite ~120 bytes of spills to L1.
+// latency-bound with half the bytes in flight per warp: 7 blocks (28 warps,
+// 72 registers) run 9 % faster despite spills to L1 (6: 3 %, 8: 7 %, 10: 3 %).
 #ifndef LBM_STEP_MIN_BLOCKS
 #define LBM_STEP_MIN_BLOCKS 5
 #endif
 #ifndef LBM_STEP_MIN_BLOCKS_16
-#define LBM_STEP_MIN_BLOCKS_16 8
+#define LBM_STEP_MIN_BLOCKS_16 7
 #endif
 template <typename S>
 __host__ __device__ constexpr int step_min_blocks() {
