@@ -167,15 +167,22 @@ inline int cell_grid(long long n) {
 // location is read once and written afterwards only by the cell that read it
 // (the AA scheme), and every value a cell stores depends on all of its loads
 // (through the density), so:
-//   * loads may take the read-only path (__ldg) or carry a prefetch hint
-//     (ld.global.L2::256B: the L2 fetches the whole 256-byte block, which the
-//     warps of neighbouring rows and slots read next);
+//   * loads carry a prefetch hint (ld.global.L2::256B: the L2 fetches the
+//     whole 256-byte block, which the warps of neighbouring rows and slots
+//     read next);
 //   * stores are streaming (st.global.cs): nothing reads them again in this
 //     launch, and the next step's reads come from HBM (the populations are
 //     five times the L2).
 __device__ __forceinline__ float load_l2(const float *p) {
   float v;
   asm volatile("ld.global.L2::256B.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
+
+// the same hint for 2-byte storage (FP16/BF16: 0.8 % faster than __ldg)
+__device__ __forceinline__ unsigned short load_l2_u16(const void *p) {
+  unsigned short v;
+  asm volatile("ld.global.L2::256B.b16 %0, [%1];" : "=h"(v) : "l"(p));
   return v;
 }
 
@@ -205,7 +212,9 @@ template <> struct Store<__half> {
   static constexpr bool DEV = true;
   template <int q> __device__ static float load(const __half *p) { return __half2float(*p); }
   template <int q> __device__ static void store(__half *p, float d) { *p = __float2half_rn(d); }
-  template <int q> __device__ static float gload(const __half *p) { return __half2float(__ldg(p)); }
+  template <int q> __device__ static float gload(const __half *p) {
+    return __half2float(__ushort_as_half(load_l2_u16(p)));
+  }
   template <int q> __device__ static void gstore(__half *p, float d) { __stcs(p, __float2half_rn(d)); }
   template <int q> __device__ static double load_value(const __half *p) {
     return (double)wq(q) + (double)__half2float(*p);
@@ -219,7 +228,9 @@ template <> struct Store<__nv_bfloat16> {
   static constexpr bool DEV = true;
   template <int q> __device__ static float load(const __nv_bfloat16 *p) { return __bfloat162float(*p); }
   template <int q> __device__ static void store(__nv_bfloat16 *p, float d) { *p = __float2bfloat16_rn(d); }
-  template <int q> __device__ static float gload(const __nv_bfloat16 *p) { return __bfloat162float(__ldg(p)); }
+  template <int q> __device__ static float gload(const __nv_bfloat16 *p) {
+    return __bfloat162float(__ushort_as_bfloat16(load_l2_u16(p)));
+  }
   template <int q> __device__ static void gstore(__nv_bfloat16 *p, float d) {
     __stcs(p, __float2bfloat16_rn(d));
   }
