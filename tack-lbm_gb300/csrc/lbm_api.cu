@@ -308,6 +308,7 @@ void release(lbm_solver *s) {
   cudaFree(c.seg_list);
   cudaFree(c.masks);
   cudaFree(c.error);
+  cudaFree(c.ticket);
   cudaFree(c.special);
   cudaFree(c.wmasks);
   cudaFree(c.fld_dev);
@@ -503,16 +504,16 @@ lbm_status lbm_create(const lbm_config *cfg, lbm_solver **out) {
     if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("heat buffers: ") + cudaGetErrorString(e)));
     s->bytes += 2 * (int64_t)gbytes + c.n * (int64_t)(sizeof(float4) + LBM_NUM_HEAT_FIELDS * sizeof(float));
   }
-  // report sums: one row per step_kernel block (at most 2 nblocks with the
-  // 64 x 2 tile) and per general block (at most nblocks / 4 + 1), or per
-  // bulk-copy block
-  c.partial_rows = std::max<int64_t>(3 * c.nblocks + 2, (int64_t)c.num_sms * 32);
+  // fast-kernel blocks plus at most one general block per four warps
+  c.partial_rows = std::max<int64_t>(2 * c.nblocks + 1, (int64_t)c.num_sms * 32);
   e = cudaMalloc(&c.fld_dev, LBM_NUM_FIELDS * sizeof(float *));
   if (e == cudaSuccess) e = cudaMemcpy(c.fld_dev, c.fld, LBM_NUM_FIELDS * sizeof(float *), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("field table: ") + cudaGetErrorString(e)));
   e = cudaMalloc(&c.partials, (size_t)c.partial_rows * lbmk::NSUM * sizeof(float2));
   if (e == cudaSuccess) e = cudaMalloc(&c.error, sizeof(unsigned int));
   if (e == cudaSuccess) e = cudaMemset(c.error, 0, sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMalloc(&c.ticket, sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMemset(c.ticket, 0, sizeof(unsigned int));
   if (e == cudaSuccess) e = cudaMalloc(&c.stage, lbmh::FINALIZE_BLOCKS * lbmk::NSUM * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&c.sums, lbmk::NSUM * sizeof(double));
   if (e == cudaSuccess) e = cudaMemset(c.sums, 0, lbmk::NSUM * sizeof(double));

@@ -508,6 +508,96 @@ __device__ __forceinline__ CSum warp_csum(float v) {
   return x;
 }
 
+// Monitor sums of a report step: the 8 summed fields (r_rho, r_ux, r_uy, r_uz,
+// r_ke, fx, fy, fz) are read back once by a streaming kernel, four cells per
+// load when n % 4 == 0. Each thread keeps compensated float pairs over its
+// cells, then warp and block pairs; every block writes 8 pairs. The last block
+// to finish (an atomic ticket, no waiting) adds the blocks' pairs in float64,
+// writes the 8 sums and resets the ticket for the next report step.
+constexpr int SUM_THREADS = 256;
+
+__device__ __forceinline__ void csum4(CSum &acc, float4 v) {
+  acc = csum_add(acc, CSum{v.x, 0.f});
+  acc = csum_add(acc, CSum{v.y, 0.f});
+  acc = csum_add(acc, CSum{v.z, 0.f});
+  acc = csum_add(acc, CSum{v.w, 0.f});
+}
+
+static __global__ void __launch_bounds__(SUM_THREADS)
+field_sums_kernel(const float *const *fld, int n, float2 *partials, unsigned int *ticket, double *sums) {
+  __shared__ CSum red[SUM_THREADS / 32][NSUM];
+  __shared__ double fin[SUM_THREADS / 32][NSUM];
+  __shared__ bool last;
+  CSum acc[NSUM];
+#pragma unroll
+  for (int k = 0; k < NSUM; ++k) acc[k] = {0.f, 0.f};
+  const float *f[NSUM];
+#pragma unroll
+  for (int k = 0; k < NSUM; ++k) f[k] = fld[5 + k];
+  const int stride = (int)gridDim.x * SUM_THREADS;
+  int tail = 0;
+  if ((n & 3) == 0) {
+    const int n4 = n >> 2;
+    for (int i = (int)blockIdx.x * SUM_THREADS + (int)threadIdx.x; i < n4; i += stride) {
+      float4 v[NSUM];
+#pragma unroll
+      for (int k = 0; k < NSUM; ++k) v[k] = reinterpret_cast<const float4 *>(f[k])[i];
+#pragma unroll
+      for (int k = 0; k < NSUM; ++k) csum4(acc[k], v[k]);
+    }
+    tail = n;
+  }
+  for (int i = tail + (int)blockIdx.x * SUM_THREADS + (int)threadIdx.x; i < n; i += stride) {
+#pragma unroll
+    for (int k = 0; k < NSUM; ++k) acc[k] = csum_add(acc[k], CSum{f[k][i], 0.f});
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NSUM; ++k) {
+    CSum x = acc[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      CSum y{__shfl_down_sync(0xffffffffu, x.hi, o), __shfl_down_sync(0xffffffffu, x.lo, o)};
+      x = csum_add(x, y);
+    }
+    if (lane == 0) red[warp][k] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < NSUM) {
+    CSum s = red[0][threadIdx.x];
+    for (int w = 1; w < SUM_THREADS / 32; ++w) s = csum_add(s, red[w][threadIdx.x]);
+    partials[(size_t)blockIdx.x * NSUM + threadIdx.x] = make_float2(s.hi, s.lo);
+    __threadfence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double d[NSUM] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += SUM_THREADS) {
+#pragma unroll
+    for (int k = 0; k < NSUM; ++k) {
+      const float2 p = __ldcg(&partials[(size_t)b * NSUM + k]);
+      d[k] += (double)p.x + (double)p.y;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < NSUM; ++k) {
+    double x = d[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) fin[warp][k] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < NSUM) {
+    double x = 0.0;
+    for (int w = 0; w < SUM_THREADS / 32; ++w) x += fin[w][threadIdx.x];
+    sums[threadIdx.x] = x;
+  }
+  if (threadIdx.x == 0) *ticket = 0u;
+}
+
 // The previous report's ux, uy, uz, p of a cell. Report steps load them with
 // the populations, before any store: the field and population pointers may
 // alias as far as the compiler knows, so a load issued after the stores would
@@ -555,27 +645,6 @@ __device__ __forceinline__ void diagnostics(float *const fld[13], int idx, const
 
 __device__ __forceinline__ int block_id() {
   return ((int)blockIdx.z * (int)gridDim.y + (int)blockIdx.y) * (int)gridDim.x + (int)blockIdx.x;
-}
-
-// A report step's monitor sums, fused into the step: each warp adds its 32
-// cells' summed values (r_rho, r_ux, r_uy, r_uz, r_ke, fx, fy, fz; the values
-// the cells store in those fields) as compensated float pairs, and the block
-// writes its 8 pairs to partial row `row`. The finalize kernels add the rows
-// in float64 in a fixed order. Every thread of the block (BX x BY) calls it.
-__device__ __forceinline__ void block_sums(float2 *partials, int row, const float v[NSUM]) {
-  __shared__ CSum red[BY][NSUM];
-#pragma unroll
-  for (int k = 0; k < NSUM; ++k) {
-    const CSum x = warp_csum(v[k]);
-    if (threadIdx.x == 0) red[threadIdx.y][k] = x;
-  }
-  __syncthreads();
-  if (threadIdx.y == 0 && threadIdx.x < NSUM) {
-    CSum s = red[0][threadIdx.x];
-#pragma unroll
-    for (int w = 1; w < BY; ++w) s = csum_add(s, red[w][threadIdx.x]);
-    partials[(size_t)row * NSUM + threadIdx.x] = make_float2(s.hi, s.lo);
-  }
 }
 
 
@@ -872,8 +941,9 @@ __host__ __device__ constexpr int step_min_blocks() {
 
 // One cell of the per-cell kernels: the warp is the 32-cell row segment at x0.
 template <typename S, int COLL, bool REPORT, bool ODD>
-__device__ __forceinline__ void cell_step(const StepArgs<S> &a, int x0, int x, int y, int z, float v[NSUM]) {
+__device__ __forceinline__ void cell_step(const StepArgs<S> &a, int x0, int x, int y, int z) {
   using T = typename Store<S>::T;
+  float v[NSUM] = {0, 0, 0, 0, 0, 0, 0, 0};
   // a warp in the obstacle's reach box whose 32 link masks are all zero (no
   // solid cell, no solid neighbour) takes the unmasked path; every lane
   // votes, including those past the lattice's end (their mask words are 0)
@@ -913,9 +983,7 @@ step_kernel(const __grid_constant__ StepArgs<S> a) {
   constexpr int TX = tile_warps_x<S>(), TY = BY / TX;
   const int wx = (int)threadIdx.y % TX, wy = (int)threadIdx.y / TX;
   const int x0 = ((int)blockIdx.x * TX + wx) * BX;
-  float v[NSUM] = {0, 0, 0, 0, 0, 0, 0, 0};
-  cell_step<S, COLL, REPORT, ODD>(a, x0, x0 + (int)threadIdx.x, (int)blockIdx.y * TY + wy, (int)blockIdx.z, v);
-  if (REPORT) block_sums(a.partials, block_id(), v);
+  cell_step<S, COLL, REPORT, ODD>(a, x0, x0 + (int)threadIdx.x, (int)blockIdx.y * TY + wy, (int)blockIdx.z);
 }
 
 // Link masks of the warps within the obstacle's reach, one warp per 32 cells.
@@ -939,7 +1007,7 @@ __global__ void warp_mask_kernel(const __grid_constant__ StepArgs<S> a, uint32_t
 
 // General kernel: the special warps, four per block, from a list of
 // (z*ny + y)*wx + x0/32 row-segment ids. Report sums go to the partial rows
-// after the step kernel's (row0 = the step kernel's block count).
+// after the fast kernel's.
 template <typename S, int COLL, bool REPORT, bool ODD>
 __global__ void __launch_bounds__(BX * BY)
 general_kernel(const __grid_constant__ StepArgs<S> a, const int *list, int count, int wx, int row0) {
@@ -954,7 +1022,7 @@ general_kernel(const __grid_constant__ StepArgs<S> a, const int *list, int count
     if (x < a.nx)
       general_cell<S, COLL, REPORT, ODD>(a, x, y, z, (z * a.ny + y) * a.nx + x, mask_slot(a, x0, y, z) >= 0, v);
   }
-  if (REPORT) block_sums(a.partials, row0 + (int)blockIdx.x, v);
+  (void)row0;
 }
 
 // ---------------------------------------------------------------------------

@@ -58,6 +58,7 @@ struct Ctx {
   uint32_t *masks;           // SW words per masked segment
   int nmasked;
   unsigned int *error;       // set by a kernel whose copy wait gave up
+  unsigned int *ticket;      // blocks of field_sums_kernel done (the last one finalizes and resets it)
   int num_sms;
   int64_t partial_rows;      // capacity of `partials` in rows of 8 doubles
 };

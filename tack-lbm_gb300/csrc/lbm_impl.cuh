@@ -87,9 +87,8 @@ cudaError_t launch_variant(const Ctx &c, const StepArgs<S> &a, cudaStream_t st, 
     if (ev) cudaEventRecord(ev[1], st);
   } else {
     const dim3 block(BX, BY);
-    constexpr int TX = tile_warps_x<S>(), TY = BY / TX;
-    const dim3 tiles((c.cfg.nx + BX * TX - 1) / (BX * TX), (c.cfg.ny + TY - 1) / TY, c.cfg.nz);
-    const int64_t fblocks = (int64_t)tiles.x * tiles.y * tiles.z;  // <= 2 nblocks: the partial rows fit
+    const dim3 grid(c.gx, c.gy, c.cfg.nz);
+    const int64_t fblocks = (int64_t)grid.x * grid.y * grid.z;
     const int gblocks = (c.nspecial + BY - 1) / BY;
     if (gblocks > 0) {
       // the special warps run beside the fast kernel: their cells' memory is disjoint
@@ -99,13 +98,23 @@ cudaError_t launch_variant(const Ctx &c, const StepArgs<S> &a, cudaStream_t st, 
                                                                          (int)fblocks);
       cudaEventRecord(c.join, c.side);
     }
-    step_kernel<S, COLL, REPORT, ODD><<<tiles, block, 0, st>>>(a);
+    {
+      constexpr int TX = tile_warps_x<S>(), TY = BY / TX;
+      const dim3 tiles((c.cfg.nx + BX * TX - 1) / (BX * TX), (c.cfg.ny + TY - 1) / TY, c.cfg.nz);
+      step_kernel<S, COLL, REPORT, ODD><<<tiles, block, 0, st>>>(a);
+    }
     if (ev) cudaEventRecord(ev[1], st);
     if (gblocks > 0) cudaStreamWaitEvent(st, c.join, 0);
-    // report steps: the kernels left one row of monitor sums per block
-    *rows = REPORT ? fblocks + gblocks : 0;
+    *rows = 0;
+    if (REPORT) {
+      // the monitor sums, read back from the fields just written
+      const int sblocks = (int)std::min<int64_t>((c.n + SUM_THREADS * 16 - 1) / (SUM_THREADS * 16),
+                                                 (int64_t)c.num_sms * 8);
+      field_sums_kernel<<<sblocks, SUM_THREADS, 0, st>>>(c.fld_dev, (int)c.n, c.partials, c.ticket, c.sums);
+      *rows = 0;  // finalized by the kernel's last block
+    }
+    (void)fblocks;
   }
-  if (REPORT && *rows > 0) launch_finalize(c, *rows, st);
   if (ev) cudaEventRecord(ev[2], st);
   return cudaGetLastError();
 }
@@ -128,7 +137,8 @@ cudaError_t launch_step(const Ctx &c, bool report, cudaStream_t st) {
     case LBM_TRT: e = launch_coll<S, COLL_TRT>(c, a, report, st, &rows); break;
     default: e = launch_coll<S, COLL_LES>(c, a, report, st, &rows); break;
   }
-  return e;
+  if (e != cudaSuccess) return e;
+  return report && rows > 0 ? launch_finalize(c, rows, st) : cudaSuccess;
 }
 
 template <typename S>
