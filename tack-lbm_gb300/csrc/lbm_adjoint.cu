@@ -693,6 +693,7 @@ lbm_status lbm_adj_set_params(lbm_adj *h, const double par[4]) {
 }
 
 lbm_status lbm_adj_forward(lbm_adj *h, double *loss) {
+  lbmh::Range range_("lbm_adj_forward");
   if (!h || !loss) return afail(LBM_ERR_ARG, "null argument");
   ACUDA(cudaSetDevice(h->cfg.device));
   lbm_status st = h->cfg.precision == LBM_F64 ? forward<double>(h) : forward<float>(h);
@@ -702,6 +703,7 @@ lbm_status lbm_adj_forward(lbm_adj *h, double *loss) {
 }
 
 lbm_status lbm_adj_backward(lbm_adj *h, double grad[4]) {
+  lbmh::Range range_("lbm_adj_backward");
   if (!h || !grad) return afail(LBM_ERR_ARG, "null argument");
   if (!h->forward_done) return afail(LBM_ERR_STATE, "lbm_adj_backward needs lbm_adj_forward with the current parameters");
   ACUDA(cudaSetDevice(h->cfg.device));

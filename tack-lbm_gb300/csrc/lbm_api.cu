@@ -547,6 +547,7 @@ lbm_status lbm_destroy(lbm_solver *s) {
   } while (0)
 
 lbm_status lbm_init(lbm_solver *s, double seed_amp) {
+  lbmh::Range range_("lbm_init");
   LBM_HANDLE(s);
   if (!std::isfinite(seed_amp)) return fail(LBM_ERR_ARG, "seed_amp must be finite");
   s->c.odd_next = 1;
@@ -556,6 +557,7 @@ lbm_status lbm_init(lbm_solver *s, double seed_amp) {
 }
 
 lbm_status lbm_init_random(lbm_solver *s, double rho_sigma, double u_noise, uint64_t seed) {
+  lbmh::Range range_("lbm_init_random");
   LBM_HANDLE(s);
   if (!std::isfinite(rho_sigma) || !std::isfinite(u_noise)) return fail(LBM_ERR_ARG, "non-finite noise");
   s->c.odd_next = 1;
@@ -565,6 +567,7 @@ lbm_status lbm_init_random(lbm_solver *s, double rho_sigma, double u_noise, uint
 }
 
 lbm_status lbm_step(lbm_solver *s, int32_t report, void *stream) {
+  lbmh::Range range_("lbm_step");
   LBM_HANDLE(s);
   LBM_CUDA(dispatch_step(s->c, report != 0, (cudaStream_t)stream));
   if (s->c.cfg.heat) {
@@ -618,6 +621,7 @@ static cudaGraphExec_t pair_graph(lbm_solver *s) {
 }
 
 lbm_status lbm_run(lbm_solver *s, int32_t count, int32_t report_last, void *stream) {
+  lbmh::Range range_("lbm_run");
   LBM_HANDLE(s);
   if (count < 0) return fail(LBM_ERR_ARG, "count must be >= 0");
   const cudaStream_t st = (cudaStream_t)stream;
@@ -664,6 +668,7 @@ lbm_status lbm_field_sums(lbm_solver *s, double out[8]) {
 }
 
 lbm_status lbm_monitors(lbm_solver *s, int32_t interval, double diameter, double out[7]) {
+  lbmh::Range range_("lbm_monitors");
   if (!out) return fail(LBM_ERR_ARG, "null output");
   double t[8];
   lbm_status st = lbm_field_sums(s, t);
@@ -864,6 +869,7 @@ lbm_status lbm_output(lbm_solver *s, int32_t id, float **ptr, int64_t *count) {
 }
 
 lbm_status lbm_update_output(lbm_solver *s, void *stream) {
+  lbmh::Range range_("lbm_update_output");
   LBM_HANDLE(s);
   LBM_CUDA(lbmh::launch_coarsen(s->c, (cudaStream_t)stream));
   return LBM_OK;
@@ -1030,6 +1036,7 @@ lbm_status lbm_set_sink(lbm_solver *s, const double sink[8]) {
 }
 
 lbm_status lbm_read_output(lbm_solver *s, int32_t id, float *host, void *stream) {
+  lbmh::Range range_("lbm_read_output");
   LBM_HANDLE(s);
   if (!host) return fail(LBM_ERR_ARG, "null host buffer");
   if (id < 0 || id >= s->c.nout)
@@ -1040,6 +1047,7 @@ lbm_status lbm_read_output(lbm_solver *s, int32_t id, float *host, void *stream)
 }
 
 lbm_status lbm_velocity_gradient(lbm_solver *s, float *jac, double inv_h, void *stream) {
+  lbmh::Range range_("lbm_velocity_gradient");
   LBM_HANDLE(s);
   if (!jac) return fail(LBM_ERR_ARG, "null gradient buffer");
   if (!std::isfinite(inv_h)) return fail(LBM_ERR_ARG, "inv_h must be finite");
@@ -1049,6 +1057,7 @@ lbm_status lbm_velocity_gradient(lbm_solver *s, float *jac, double inv_h, void *
 
 lbm_status lbm_vorticity_q(lbm_solver *s, const float *jac, float *vorticity, float *q, int32_t at_cells,
                            void *stream) {
+  lbmh::Range range_("lbm_vorticity_q");
   LBM_HANDLE(s);
   if (!jac) return fail(LBM_ERR_ARG, "null gradient buffer");
   if (at_cells != 0 && at_cells != 1) return fail(LBM_ERR_ARG, "at_cells must be 0 or 1");
@@ -1057,6 +1066,7 @@ lbm_status lbm_vorticity_q(lbm_solver *s, const float *jac, float *vorticity, fl
 }
 
 lbm_status lbm_run_timed(lbm_solver *s, int32_t count, int32_t report_last, void *stream, double *ms) {
+  lbmh::Range range_("lbm_run_timed");
   LBM_HANDLE(s);
   if (!ms) return fail(LBM_ERR_ARG, "null output");
   cudaEvent_t ev[2] = {nullptr, nullptr};

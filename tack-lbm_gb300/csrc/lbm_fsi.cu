@@ -471,6 +471,7 @@ lbm_status lbm_fsi_init(lbm_fsi *w, const double *kin) {
 }
 
 lbm_status lbm_fsi_step(lbm_fsi *w, int32_t report, const double *kin, double *load) {
+  lbmh::Range range_("lbm_fsi_step");
   if (!w || !kin || !load) return ffail(LBM_ERR_ARG, "null argument");
   FCUDA(cudaSetDevice(w->cfg.device));
   lbm_status st = set_kin(w, kin);

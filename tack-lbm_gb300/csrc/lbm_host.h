@@ -8,7 +8,35 @@
 
 #include "../../include/lbm_gb300.h"
 
+#if defined(__has_include)
+#if __has_include(<nvtx3/nvToolsExt.h>)
+#include <nvtx3/nvToolsExt.h>
+#define LBM_HAVE_NVTX 1
+#endif
+#endif
+
 namespace lbmh {
+
+// An NVTX range over one C-ABI call, named after the entry point, so that
+// timeline and kernel profilers can group a step's launches (ncu --nvtx
+// --nvtx-include "lbm_step/"). NVTX is header-only and does nothing unless a
+// tool is attached; without the header the range is empty.
+struct Range {
+  explicit Range(const char *name) {
+#ifdef LBM_HAVE_NVTX
+    nvtxRangePushA(name);
+#else
+    (void)name;
+#endif
+  }
+  ~Range() {
+#ifdef LBM_HAVE_NVTX
+    nvtxRangePop();
+#endif
+  }
+  Range(const Range &) = delete;
+  Range &operator=(const Range &) = delete;
+};
 
 // Everything the launch helpers need about one solver.
 struct Ctx {

@@ -317,6 +317,7 @@ lbm_status lbm_wing_init(lbm_wing *w, const double state[4]) {
 }
 
 lbm_status lbm_wing_step(lbm_wing *w, int32_t report, const double state[4], double load[3]) {
+  lbmh::Range range_("lbm_wing_step");
   if (!w || !state || !load) return wfail(LBM_ERR_ARG, "null argument");
   WCUDA(cudaSetDevice(w->cfg.device));
   lbm_status st = build_mask(w, state);
