@@ -217,19 +217,29 @@ def cpu_baseline_single(f, target_s=12.0):
 # reference arm: the CPU restatement over all host cores
 
 def _worker(args):
-    shm_name, shape, lo, hi = args
+    """``reps`` oracle passes over cells [lo, hi) of the shared population array."""
+    shm_name, shape, lo, hi, reps = args
     from multiprocessing import shared_memory
     shm = shared_memory.SharedMemory(name=shm_name)
     try:
         f = np.ndarray(shape, dtype=np.float32, buffer=shm.buf)
+        cells = np.arange(lo, hi)
         t0 = time.perf_counter()
-        cpu_sample_step(f, np.arange(lo, hi))
+        for _ in range(reps):
+            cpu_sample_step(f, cells)
         return time.perf_counter() - t0
     finally:
         shm.close()
 
 
 def run_reference(args):
+    """The reference arm: the float32 NumPy oracle on every host core.
+
+    Each step is one oracle pass over a sample of the workload's cells, split
+    over a spawn-started process pool; every worker runs all of its steps in
+    one dispatch, so the pool costs nothing per step. The sample is sized by a
+    one-plane calibration pass so that warm-up plus timed steps take about
+    ``--ref-seconds`` (between 1024 cells per core and two z-planes per step)."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1 and rank != 0:
@@ -247,25 +257,31 @@ def run_reference(args):
         del f0
         cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
         nxy = w["nx"] * w["ny"]
-        # each step: one oracle pass over a sample of z-planes, split across all cores
-        planes = max(1, min(w["nz"], int(os.environ.get("LBM_REF_PLANES", "2"))))
-        sample = planes * nxy
-        bounds = np.linspace(0, sample, cores + 1).astype(int)
-        jobs = [(shm.name, f.shape, int(bounds[i]), int(bounds[i + 1])) for i in range(cores)]
+
+        def jobs(sample, reps):
+            bounds = np.linspace(0, sample, cores + 1).astype(int)
+            return [(shm.name, f.shape, int(bounds[i]), int(bounds[i + 1]), reps) for i in range(cores)]
+
         ctx = mp.get_context("spawn")
         with ctx.Pool(cores) as pool:
-            for _ in range(args.warmup):
-                pool.map(_worker, jobs)
+            pool.map(_worker, jobs(nxy, 1))  # imports, page-in
             t0 = time.perf_counter()
-            for _ in range(args.steps):
-                pool.map(_worker, jobs)
+            pool.map(_worker, jobs(nxy, 1))
+            per_cell = (time.perf_counter() - t0) / nxy
+            total = args.steps + args.warmup
+            sample = int(args.ref_seconds / (total * per_cell))
+            sample = max(cores * 1024, min(2 * nxy, sample))
+            pool.map(_worker, jobs(sample, args.warmup))
+            t0 = time.perf_counter()
+            pool.map(_worker, jobs(sample, args.steps))
             dt = time.perf_counter() - t0
     finally:
         shm.close()
         shm.unlink()
     value = sample * args.steps / dt / 1e9
-    desc = (f"one float32 NumPy oracle pass over {planes} z-plane(s) ({sample} cells) of the workload "
-            f"per step, split over {cores} processes")
+    desc = (f"one float32 NumPy oracle pass over {sample} cells of the workload (the first "
+            f"{sample / nxy:.2f} z-planes) per step, split over {cores} processes; sample sized for "
+            f"~{args.ref_seconds:.0f} s of warm-up and timed steps")
     line = {"impl": "reference", "metric": "GLUPS", "value": value, "unit": "GLUPS", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -441,6 +457,8 @@ def main():
     ap.add_argument("--steps", type=int, default=4000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--ref-seconds", type=float, default=60.0,
+                    help="reference arm: size the per-step CPU sample so warm-up + timed steps take about this")
     ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16", "f64"])
     ap.add_argument("--path", default="auto", choices=["auto", "simt", "bulkcopy"],
                     help="step kernel: per-cell (auto, simt) or bulk-copy staged (bulkcopy)")
