@@ -354,7 +354,9 @@ lbm_status lbm_wing_set_physics(lbm_wing *w, int32_t collision, double nu);
 lbm_status lbm_wing_field(lbm_wing *w, int32_t id, float **ptr);
 /* Copy the current populations (19 n floats, f[q*n + idx]) from (set = 0) or to (set = 1) `host`. */
 lbm_status lbm_wing_populations(lbm_wing *w, float *host, int32_t set);
-/* The solid mask (n bytes) at `state`. */
+/* The solid mask (n bytes) at `state`: the section test of flutter.py:30-42 with
+ * float64 results (a float32 prefilter decides the points away from the outline,
+ * the rest run in float64), as every step uses it. */
 lbm_status lbm_wing_mask(lbm_wing *w, const double state[4], uint8_t *host);
 /* Output grid: the five fields subsampled by `stride` (flutter.py:207-211). */
 lbm_status lbm_wing_set_output_stride(lbm_wing *w, int32_t stride);
@@ -391,6 +393,8 @@ lbm_status lbm_fsi_step(lbm_fsi *w, int32_t report, const double *kin, double *l
 lbm_status lbm_fsi_set_physics(lbm_fsi *w, int32_t collision, double nu);
 lbm_status lbm_fsi_field(lbm_fsi *w, int32_t id, float **ptr);
 lbm_status lbm_fsi_populations(lbm_fsi *w, float *host, int32_t set);
+/* The solid mask (n bytes) at the layer kinematics kin (fsi.py:35-47), with
+ * float64 results as in lbm_wing_mask; kin becomes the handle's kinematics. */
 lbm_status lbm_fsi_mask(lbm_fsi *w, const double *kin, uint8_t *host);
 lbm_status lbm_fsi_set_output_stride(lbm_fsi *w, int32_t stride);
 lbm_status lbm_fsi_output(lbm_fsi *w, int32_t id, float **ptr, int64_t *count);
