@@ -79,8 +79,9 @@ class Clocks:
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index):
+    def __init__(self, index, period_ms=20):
         self.index = index
+        self.period_ms = period_ms
         self.proc = None
         self.lines = []
 
@@ -88,7 +89,7 @@ class Clocks:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", str(self.period_ms)],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -279,14 +280,19 @@ def run_reference(args):
         shm.close()
         shm.unlink()
     value = sample * args.steps / dt / 1e9
+    n = w["nx"] * w["ny"] * w["nz"]
+    sample_ms = dt / args.steps * 1e3
     desc = (f"one float32 NumPy oracle pass over {sample} cells of the workload (the first "
             f"{sample / nxy:.2f} z-planes) per step, split over {cores} processes; sample sized for "
             f"~{args.ref_seconds:.0f} s of warm-up and timed steps")
     line = {"impl": "reference", "metric": "GLUPS", "value": value, "unit": "GLUPS", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "steps": args.steps, "warmup": args.warmup,
+            # one step of the whole lattice at the sample's rate; the sample's own time beside it
+            "ms_per_step": sample_ms * n / sample, "sample_ms_per_step": sample_ms, "sample_cells": sample,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": workload_config("f32"),
-            "cpu_baseline": {"value": value, "unit": "GLUPS", "cores": cores, "kind": "port", "sample": desc},
+            "cpu_baseline": {"value": value, "unit": "GLUPS", "cores": cores, "kind": "port", "sample": desc,
+                             "cpu_model": cpu_model()},
             "e2e": {"value": value, "unit": "GLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "gpu_launches": 0}
     print(json.dumps(line), flush=True)
@@ -308,13 +314,32 @@ def adjoint_timing(device):
     loss = run.forward()
     grad = run.backward()
     info = run.info()
+    del run
     cells = 256 * 128 * 32
+    prod_ms = production_forward_ms(device)
     return {"workload": "LES cylinder Re 100, 256x128x32, 2000 steps, K=100, FP32",
             "loss": loss, "grad": {k: float(v) for k, v in zip(("U", "tau0", "Cs", "r"), grad)},
             "forward_ms": info["forward_ms"], "backward_ms": info["backward_ms"],
             "backward_over_forward": info["backward_ms"] / info["forward_ms"],
             "forward_glups": cells * 2000 / (info["forward_ms"] * 1e-3) / 1e9,
+            "production_forward_ms": prod_ms,
+            "backward_over_production_forward": info["backward_ms"] / prod_ms,
+            "production_forward": "2000 quiet steps of the production step kernel (Solver, FP32, AA in place) "
+                                  "on the same lattice: LES Re 100, cylinder r 8 at (0.22 nx, 0.5 ny + 1.7), "
+                                  "U 0.05, Cs 0.1, one lbm_run_timed",
             "device_bytes": info["device_bytes"]}
+
+
+def production_forward_ms(device, steps=2000):
+    """CUDA-event time of ``steps`` quiet production steps (step_kernel) on the
+    adjoint's lattice and flow: the forward cost the backward pass is held to."""
+    import lbm
+    s = lbm.Solver(256, 128, 32, collision="les", reynolds=100.0, u0=0.05, diameter=16.0, cs=0.1,
+                   device=f"cuda:{device}")
+    ms = ctypes.c_double()
+    s._h.call("lbm_run_timed", 50, 0, None, ctypes.byref(ms))
+    s._h.call("lbm_run_timed", int(steps), 0, None, ctypes.byref(ms))
+    return ms.value
 
 
 # ---------------------------------------------------------------------------
@@ -340,6 +365,7 @@ def _coupled(step, count, torch):
 
 
 NEXT_ROWS = ("heat", "flutter", "fsi", "derived")
+STUDY_NAMES = ("c2", "c3", "c5", "collision", "drag_window")
 
 
 def row_heat(device, peak, torch):
@@ -451,80 +477,65 @@ def next_rows(device, peak, torch, solver, rows=NEXT_ROWS):
     return out
 
 
-def main():
-    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=4000)
-    ap.add_argument("--warmup", type=int, default=20)
-    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--ref-seconds", type=float, default=60.0,
-                    help="reference arm: size the per-step CPU sample so warm-up + timed steps take about this")
-    ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16", "f64"])
-    ap.add_argument("--path", default="auto", choices=["auto", "simt", "bulkcopy"],
-                    help="step kernel: per-cell (auto, simt) or bulk-copy staged (bulkcopy)")
-    ap.add_argument("--e2e-steps", type=int, default=500)
-    ap.add_argument("--report", action="store_true",
-                    help="time report steps (13 diagnostic fields and FP64 monitor sums every step)")
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--study", choices=["c2", "c3", "c5"],
-                    help="run a physics/precision study instead of the benchmark (one JSON line)")
-    ap.add_argument("--study-steps", type=int, default=None)
-    ap.add_argument("--no-adjoint", action="store_true",
-                    help="skip the drag-adjoint timing (256x128x32, 2000 steps, FP32)")
-    ap.add_argument("--no-next-rows", action="store_true",
-                    help="skip the heat, flutter, FSI and derived-field timings")
-    ap.add_argument("--next-rows-only", default=None, metavar="ROWS",
-                    help="time only these widened rows (comma list of heat,flutter,fsi,derived) and print "
-                         "one JSON line with them")
-    args = ap.parse_args()
-    if args.warmup < 3:
-        ap.error("--warmup must be >= 3")
-    if args.impl == "reference":
-        return run_reference(args)
-    if args.study:
-        import studies
-        kw = {} if args.study_steps is None else {"steps": args.study_steps}
-        print(json.dumps(studies.STUDIES[args.study](**kw)), flush=True)
-        return 0
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else platform)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":")[0].strip() == "Model name":
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
 
-    world, rank, local, dist, torch = dist_setup(args.gpus)
-    import lbm_native as N
-    if args.next_rows_only:
-        import torch as torch_host
-        rows = [r.strip() for r in args.next_rows_only.split(",") if r.strip()]
-        bad = [r for r in rows if r not in NEXT_ROWS]
-        if bad:
-            ap.error(f"unknown rows {bad}; choose from {NEXT_ROWS}")
-        s = make_solver(args.storage, local, args.path) if "derived" in rows else None
-        peak, _ = peaks()
-        print(json.dumps({"next_rows": next_rows(local, peak, torch_host, s, rows)}), flush=True)
-        return 0
-    s = make_solver(args.storage, local, args.path)
+
+# The kernel-timing pass (every step's kernels between CUDA events) runs right
+# before the timed region, long enough for the clock sampler to see the GPU
+# under load whatever --steps is: at least this many seconds of steps.
+CLOCK_WINDOW_S = 0.5
+
+
+def device_leg(s, args, storage, local, dist=None, torch=None, world=1):
+    """Warm-up, a kernel-timing pass and the timed region of one solver.
+
+    Returns (value, span_ms, roofline, step_roofline, clocks, extra): value in
+    GLUPS over the timed region (K steps between two CUDA events on the launch
+    stream), the dominant kernel's roofline from the event-bracketed pass."""
     steps = args.steps
     for _ in range(args.warmup):
         s.step(report=args.report)
     s.sync()
-    # kernel durations for the roofline: a separate pass with every step's
-    # kernels bracketed by CUDA events (lbm_timing)
-    kernel_steps = min(steps, 1000)
-    s._h.call("lbm_timing", 1)
-    for _ in range(kernel_steps):
-        s.step(report=args.report)
-    s.sync()
-    t = (ctypes.c_double * 7)()
-    s._h.call("lbm_timing_read", t)
-    s._h.call("lbm_timing", 0)
 
-    # the timed region: K steps between two CUDA events on the launch stream
-    # (lbm_run_timed; quiet steps go as CUDA graphs of step pairs), no events
-    # in between; report steps one lbm_run_timed each, their device times summed
     def run_timed(count, report_last):
         ms = ctypes.c_double()
         s._h.call("lbm_run_timed", int(count), int(report_last), None, ctypes.byref(ms))
         return ms.value
 
+    # one probe step sizes the kernel-timing pass to CLOCK_WINDOW_S (capped by
+    # the 4096 event slots of lbm_timing)
+    probe = run_timed(20, 0) / 20 if not args.report else run_timed(1, 1)
+    kernel_steps = int(min(4000, max(min(steps, 1000), CLOCK_WINDOW_S / max(probe * 1e-3, 1e-6))))
+    t = (ctypes.c_double * 7)()
     barrier(dist, torch)
     with Clocks(local) as clocks:
+        s._h.call("lbm_timing", 1)
+        for _ in range(kernel_steps):
+            s.step(report=args.report)
+        s.sync()
+        s._h.call("lbm_timing_read", t)
+        s._h.call("lbm_timing", 0)
+        # the timed region: K steps between two CUDA events on the launch
+        # stream (lbm_run_timed; quiet steps go as CUDA graphs of step pairs),
+        # no events in between; report steps one lbm_run_timed each
+        barrier(dist, torch)
         t0 = time.perf_counter()
         if args.report:
             span_ms = sum(run_timed(1, 1) for _ in range(steps))
@@ -540,15 +551,134 @@ def main():
     kernel_name = "stream_kernel (bulk-copy)" if args.path == "bulkcopy" else "step_kernel"
     solid = int(s.mask().sum())
     # a report step also reads 4 and writes 13 float32 fields per cell (lbm.py:493-513)
-    bytes_cell = BYTES_PER_CELL[args.storage] + (68 if args.report else 0)
+    bytes_cell = BYTES_PER_CELL[storage] + (68 if args.report else 0)
     # the dominant kernel updates t[2] cells (all but lid rows); its obstacle
     # cells move no bytes on a quiet step, every fluid cell moves bytes_cell
     kernel_bytes = bytes_cell * (t[2] - solid)
     achieved = kernel_bytes / (bulk_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
     step_bytes = bytes_cell * (cells - solid)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs (burst copy)",
+                "traffic": (NCU_TRAFFIC.get((storage, bool(args.report)))
+                            if args.path != "bulkcopy" else None),
+                "traffic_unit": "B per launch (ncu dram read + write)",
+                "kernel": kernel_name, "bytes_per_cell": bytes_cell,
+                "fluid_cells_per_launch": int(t[2] - solid), "ms_per_launch": bulk_ms,
+                "timed_launches": kernel_steps}
+    step_roofline = {"achieved": step_bytes / (span_ms / steps * 1e-3) / 1e9,
+                     "frac": step_bytes / (span_ms / steps * 1e-3) / 1e9 / peak,
+                     "lid_row_cells": int(t[5])}
+    ck = clocks.summary()
+    ck["window"] = (f"kernel-timing pass ({kernel_steps} steps, {t[6]:.0f} ms) + the timed region "
+                    f"({steps} steps, {span_ms:.1f} ms), sampled every 20 ms")
+    extra = {"wall_s": wall, "lid_row_cells": int(t[5]), "solid": solid}
+    return value, span_ms, roofline, step_roofline, ck, extra
 
-    # end to end through the public API: a report step and monitors() every step
+
+def storage_variants(args, local, f32_value, storages=("f16", "bf16")):
+    """The FP16/BF16 deviation-storage legs on the same workload, steps and
+    warm-up as the FP32 line: GLUPS, ms per step and the step kernel's
+    roofline (76 B per fluid cell)."""
+    out = {}
+    for st in storages:
+        s = make_solver(st, local, args.path)
+        value, span_ms, roof, step_roof, ck, _ = device_leg(s, args, st, local)
+        out[st] = {"value": value, "unit": "GLUPS", "ms_per_step": span_ms / args.steps,
+                   "dtype": DTYPE[st], "roofline": roof, "step_roofline": step_roof, "clocks": ck,
+                   "config": workload_config(st, args.report)}
+        del s
+    for st in storages:
+        out[f"{st}_over_f32"] = out[st]["value"] / f32_value
+    return out
+
+
+def reference_workload(local, warmup=5, steps=200):
+    """tack-lbm's own benchmark (bench.py:9-23 there) through the drop-in: the
+    default Solver (384 x 128 x 64, LES, Re 300, cylinder D = 24, U = 0.08,
+    periodic y and z, lbm_init start), ``warmup`` steps, then ``steps`` quiet
+    Solver.step() calls timed by the host clock with a sync on both sides."""
+    import lbm
+    t0 = time.perf_counter()
+    s = lbm.Solver(collision="les", device=f"cuda:{local}")
+    s.sync()
+    setup = time.perf_counter() - t0
+    for _ in range(warmup):
+        s.step()
+    s.sync()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        s.step()
+    s.sync()
+    dt = time.perf_counter() - t0
+    m = s.monitors(steps)
+    return {"workload": "tack-lbm bench.py: default Solver, LES Re 300, 384x128x64, cylinder D 24, "
+                        f"{warmup} warm-up + {steps} timed Solver.step() calls",
+            "steps_per_s": steps / dt, "mlups": s.lat.n * steps / dt / 1e6,
+            "glups": s.lat.n * steps / dt / 1e9, "ms_per_step": dt / steps * 1e3,
+            "setup_s": setup, "timing": "host clock around the Solver.step() calls, synced both sides",
+            "monitors_finite": bool(np.isfinite(list(m.values())).all())}
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=4000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--ref-seconds", type=float, default=60.0,
+                    help="reference arm: size the per-step CPU sample so warm-up + timed steps take about this")
+    ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16", "f64"])
+    ap.add_argument("--path", default="auto", choices=["auto", "simt", "bulkcopy"],
+                    help="step kernel: per-cell (auto, simt) or bulk-copy staged (bulkcopy)")
+    ap.add_argument("--e2e-steps", type=int, default=500)
+    ap.add_argument("--report", action="store_true",
+                    help="time report steps (13 diagnostic fields and FP64 monitor sums every step)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--study", choices=sorted(STUDY_NAMES),
+                    help="run a physics/precision study instead of the benchmark (one JSON line)")
+    ap.add_argument("--study-steps", type=int, default=None)
+    ap.add_argument("--no-adjoint", action="store_true",
+                    help="skip the drag-adjoint timing (256x128x32, 2000 steps, FP32)")
+    ap.add_argument("--no-next-rows", action="store_true",
+                    help="skip the heat, flutter, FSI and derived-field timings")
+    ap.add_argument("--no-variants", action="store_true",
+                    help="skip the FP16/BF16 storage legs and the reference-workload leg")
+    ap.add_argument("--next-rows-only", default=None, metavar="ROWS",
+                    help="time only these widened rows (comma list of heat,flutter,fsi,derived) and print "
+                         "one JSON line with them")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.study:
+        import studies
+        kw = {} if args.study_steps is None else {"steps": args.study_steps}
+        print(json.dumps(studies.STUDIES[args.study](**kw)), flush=True)
+        return 0
+
+    world, rank, local, dist, torch = dist_setup(args.gpus)
+    import lbm_native as N  # noqa: F401  (loads the library, fails loudly without it)
+    if args.next_rows_only:
+        import torch as torch_host
+        rows = [r.strip() for r in args.next_rows_only.split(",") if r.strip()]
+        bad = [r for r in rows if r not in NEXT_ROWS]
+        if bad:
+            ap.error(f"unknown rows {bad}; choose from {NEXT_ROWS}")
+        s = make_solver(args.storage, local, args.path) if "derived" in rows else None
+        peak, _ = peaks()
+        print(json.dumps({"next_rows": next_rows(local, peak, torch_host, s, rows)}), flush=True)
+        return 0
+    s = make_solver(args.storage, local, args.path)
+    steps = args.steps
+    value, span_ms, roofline, step_roofline, clocks, extra = device_leg(s, args, args.storage, local, dist,
+                                                                        torch, world)
+    cells = s.lat.n
+    peak, _ = peaks()
+
+    # end to end through the public API: a report step and monitors() every
+    # E2E_INTERVAL steps, the output fields copied to pinned host memory
     intervals = max(1, args.e2e_steps // E2E_INTERVAL)
     import torch as torch_host  # pinned host buffers only
     host_out = {k: torch_host.empty(s.output[k].numpy.size, dtype=torch_host.float32).pin_memory().numpy()
@@ -588,29 +718,26 @@ def main():
                         "Solver.read_output() of the 5 output fields into pinned host memory, "
                         "Solver.set_actuation()"),
                 "steps": e2e_steps, "ms_per_step": e2e_wall / e2e_steps * 1e3},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs (burst copy)",
-                     "traffic": (NCU_TRAFFIC.get((args.storage, bool(args.report)))
-                                 if args.path != "bulkcopy" else None),
-                     "traffic_unit": "B per launch (ncu dram read + write)",
-                     "kernel": kernel_name, "bytes_per_cell": bytes_cell,
-                     "fluid_cells_per_launch": int(t[2] - solid), "ms_per_launch": bulk_ms,
-                     "timed_launches": kernel_steps},
-        "step_roofline": {"achieved": step_bytes / (span_ms / steps * 1e-3) / 1e9,
-                          "frac": step_bytes / (span_ms / steps * 1e-3) / 1e9 / peak,
-                          "lid_row_cells": int(t[5])},
-        "gpu_launches": steps * (2 if t[5] > 0 else 1) + (steps if args.report else 0),
-        "clocks": clocks.summary(),
+        "roofline": roofline,
+        "step_roofline": step_roofline,
+        "gpu_launches": steps * (2 if extra["lid_row_cells"] > 0 else 1) + (steps if args.report else 0),
+        "clocks": clocks,
         "monitors_finite": bool(finite),
-        "wall_s": wall,
+        "wall_s": extra["wall_s"],
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         f = s.populations(np.float32)
         line["cpu_baseline"] = cpu_baseline_single(f)
+        line["cpu_baseline"]["cpu_model"] = cpu_model()
+        line["cpu_baseline"]["host_cores"] = os.cpu_count()
     if world == 1 and not args.no_next_rows:
         line["next_rows"] = next_rows(local, peak, torch_host, s)
+    del s
+    if world == 1 and not args.no_variants:
+        if args.storage == "f32" and not args.report:
+            line["storage_variants"] = storage_variants(args, local, value)
+        line["reference_workload"] = reference_workload(local)
     if not args.no_adjoint:
-        del s
         line["adjoint"] = adjoint_timing(local)
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -509,6 +509,14 @@ def weight_err(a, b):
 # by central differences, one-sided at the grid's faces, and the default
 # fields |curl u| and Q = -1/2 J_ij J_ji (derived.py:27-30).
 
+def coarsen(field, dims, stride):
+    """The output grid of a field (lbm.py:516-522): every ``stride``-th cell along
+    each axis, starting at 0; ceil(n / stride) points per axis."""
+    nx, ny, nz = dims
+    a = np.asarray(field).reshape(nz, ny, nx)
+    return np.ascontiguousarray(a[::stride, ::stride, ::stride]).reshape(-1)
+
+
 def velocity_gradient(ux, uy, uz, dims, inv_h):
     """(m, 3, 3) array, [p, c, d] = d u_c / d x_d at output point p."""
     mx, my, mz = dims

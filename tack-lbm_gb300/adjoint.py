@@ -90,6 +90,7 @@ class DragAdjoint:
         p = np.ascontiguousarray(np.asarray(params, np.float64).reshape(4))
         N.check(self.lib.lbm_adj_set_params(self.ptr, p.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         self.params = p.copy()
+        self.loss = None  # no forward pass at these parameters yet
 
     def forward(self):
         """Run all steps from the start state; returns the loss."""
@@ -119,17 +120,29 @@ class DragAdjoint:
 
 
 class DragLoss(torch.autograd.Function):
-    """loss = DragLoss.apply(params, run): params = (U, tau0, Cs, r) as a 4-tensor."""
+    """loss = DragLoss.apply(params, run): params = (U, tau0, Cs, r) as a 4-tensor.
+
+    Each application keeps its own parameters. The run holds the checkpoints
+    of its last forward pass only, so when ``run`` has been applied again at
+    other parameters before this loss's ``backward`` (a line search, two
+    losses in one graph), ``backward`` first reruns the forward pass at this
+    application's parameters; the gradient is always that of this loss."""
 
     @staticmethod
     def forward(ctx, params, run):
-        run.set_params(params.detach().to("cpu", torch.float64).numpy())
+        p = params.detach().to("cpu", torch.float64).numpy().copy()
+        run.set_params(p)
         ctx.run = run
+        ctx.params = p
         return params.new_tensor(run.forward())
 
     @staticmethod
     def backward(ctx, grad_out):
-        g = torch.as_tensor(ctx.run.backward(), dtype=grad_out.dtype, device=grad_out.device)
+        run = ctx.run
+        if run.loss is None or not np.array_equal(run.params, ctx.params):
+            run.set_params(ctx.params)
+            run.forward()
+        g = torch.as_tensor(run.backward(), dtype=grad_out.dtype, device=grad_out.device)
         return grad_out * g, None
 
 

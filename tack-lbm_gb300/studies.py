@@ -17,6 +17,12 @@ of results. ``bench.py --study c2|c3|c5`` prints them as one JSON line.
   box 64x64x128 at (256, 256, 128), lid u = 0.05, U = 0.08): FP16 against
   FP32 throughput and drag at full size, and the drag error of FP16 and FP32
   against FP64 on the 256x128x64 downsample of the same flow.
+* ``study_collision``: tack-lbm's collision_check.py (collision_check.py:9-31)
+  through the drop-in: stability and Strouhal number of bgk/trt/les at
+  Re 300, 1000 and 3000 on the default Solver.
+* ``study_drag_window``: FP32/FP16/BF16 time-averaged drag against FP64 over
+  growing windows, with FP32's own error showing where trajectory divergence
+  starts to dominate.
 
 The time-averaged drag is the mean of the drag monitor (Solver.monitors,
 lbm.py:649-661) over the second half of the run.
@@ -190,4 +196,120 @@ def study_c5(steps=5000, every=100, device=0):
     return out
 
 
-STUDIES = {"c2": study_c2, "c3": study_c3, "c5": study_c5}
+def _collision_run(collision, re, steps, every, device):
+    """One collision_check.py run (collision_check.py:12-31): the default Solver
+    (384x128x64, cylinder D = 24, U = 0.08, periodic y and z, lbm_init start) at
+    Reynolds number ``re``, ``every - 1`` quiet steps and one report step per
+    block, monitors(every), stop at the first non-finite drag. The Strouhal
+    number is the raw rFFT peak of the mean-removed lift over the second half
+    of the history (collision_check.py:27-30), with its bin width, and the
+    Hann-windowed, parabola-refined peak of ``strouhal``."""
+    s = lbm.Solver(collision=collision, reynolds=float(re), device=device)
+    lift, blew_up = [], None
+    t0 = time.perf_counter()
+    for _ in range(steps // every):
+        s.run(every, report_last=True)
+        m = s.monitors(every)
+        if not np.isfinite(m["drag"]):
+            blew_up = s.step_count
+            break
+        lift.append(m["lift"])
+    wall = time.perf_counter() - t0
+    r = {"collision": collision, "reynolds": re, "steps": steps, "report_every": every,
+         "glups_wall": s.lat.n * s.step_count / wall / 1e9}
+    if blew_up is not None:
+        r.update(stable=False, diverged_at_step=blew_up)
+        return r
+    cl = np.array(lift[len(lift) // 2:])
+    cl -= cl.mean()
+    spec = np.abs(np.fft.rfft(cl))
+    freq = np.fft.rfftfreq(len(cl), d=every)
+    k = int(np.argmax(spec[1:]) + 1)
+    scale = s.diameter / s.u0
+    r.update(stable=True, cl_amplitude=float(np.abs(cl).max()), strouhal_raw=float(freq[k] * scale),
+             strouhal_bin=float(freq[1] * scale), strouhal_refined=strouhal(cl, every, s.diameter, s.u0))
+    return r
+
+
+def study_collision(steps=8000, every=50, long_steps=30000, device=0):
+    """tack-lbm's collision_check.py through the drop-in: bgk/trt/les at
+    Re 300, 1000 and 3000 (8000 steps, a report every 50). The reference's
+    documented answers (README.md:63-67): St = 0.200 for all three models at
+    Re 300, BGK diverges at Re 3000, TRT and LES stay stable. With 8000 steps
+    the raw rFFT grid is St = k * 0.075, so Re 300 is also run for
+    ``long_steps`` steps (a finer grid)."""
+    out = {"study": "collision", "workload": "collision_check.py: default Solver 384x128x64, cylinder D 24, "
+           "U 0.08, periodic y and z", "steps": steps, "report_every": every, "runs": []}
+    for re in (300, 1000, 3000):
+        for coll in ("bgk", "trt", "les"):
+            out["runs"].append(_collision_run(coll, re, steps, every, device))
+    if long_steps:
+        out["long"] = [_collision_run(coll, 300, long_steps, every, device) for coll in ("bgk", "trt", "les")]
+    runs = {(r["reynolds"], r["collision"]): r for r in out["runs"]}
+    out["checks"] = {
+        "bgk_diverges_at_re3000": not runs[(3000, "bgk")]["stable"],
+        "trt_les_stable_at_re3000": runs[(3000, "trt")]["stable"] and runs[(3000, "les")]["stable"],
+        "re300_strouhal_within_one_bin_of_0.200": all(
+            r["stable"] and abs(r["strouhal_raw"] - 0.2) <= r["strouhal_bin"] for r in out["runs"]
+            if r["reynolds"] == 300),
+    }
+    if long_steps:
+        out["checks"]["re300_long_strouhal_within_one_bin_of_0.200"] = all(
+            r["stable"] and abs(r["strouhal_raw"] - 0.2) <= r["strouhal_bin"] for r in out["long"])
+    return out
+
+
+def _drag_history(s, steps, every):
+    t, drag = [], []
+    done = 0
+    while done < steps:
+        k = min(every, steps - done)
+        s.run(k, report_last=True)
+        done += k
+        t.append(done)
+        drag.append(s.monitors(k)["drag"])
+    return np.array(t), np.array(drag)
+
+
+def study_drag_window(steps=4000, every=10, device=0, cases=("c5_downsample", "c3")):
+    """Storage error of the time-averaged drag, measured where it can be seen.
+
+    Each case runs FP64, FP32, FP16 and BF16 storage from the same start state
+    with the drag monitor every ``every`` steps. For each window end N (a
+    quarter, half, three quarters and all of ``steps``) the time-averaged drag
+    over steps (N/2, N] of every storage is compared with FP64's. FP32's own
+    error in a window bounds what trajectory divergence (not storage
+    precision) contributes there; a window where FP32 agrees with FP64 to
+    well under 1e-3 isolates FP16/BF16's storage error.
+
+    * c5_downsample: the LES box at Re 3000 with the moving lid, 256x128x64
+      (the 1024x512x256 configuration scaled by 1/4), seeded noise;
+    * c3: the TRT + Smagorinsky sphere at Re 1000, 768x384x128, r = 24,
+      U = 0.06, Cs = 0.16 (Cs = 0.1 diverges in FP64 too)."""
+    out = {"study": "drag_window", "steps": steps, "report_every": every, "cases": {}}
+    for case in cases:
+        hist = {}
+        for st in ("f64", "f32", "f16", "bf16"):
+            s = _c5_solver(st, 4, device) if case == "c5_downsample" else _c3_solver(st, device, 0.16)
+            t0 = time.perf_counter()
+            t, drag = _drag_history(s, steps, every)
+            hist[st] = (t, drag, time.perf_counter() - t0)
+            del s
+        windows = []
+        for frac in (0.25, 0.5, 0.75, 1.0):
+            n_end = int(round(steps * frac / every)) * every
+            sel = (hist["f64"][0] > n_end // 2) & (hist["f64"][0] <= n_end)
+            ref = float(hist["f64"][1][sel].mean())
+            w = {"window": [n_end // 2 + 1, n_end], "f64_drag": ref}
+            for st in ("f32", "f16", "bf16"):
+                cd = float(hist[st][1][sel].mean())
+                w[f"{st}_drag_rel_err"] = abs(cd - ref) / abs(ref)
+            windows.append(w)
+        out["cases"][case] = {"windows": windows,
+                              "finite": {st: bool(np.isfinite(h[1]).all()) for st, h in hist.items()},
+                              "wall_s": {st: h[2] for st, h in hist.items()}}
+    return out
+
+
+STUDIES = {"c2": study_c2, "c3": study_c3, "c5": study_c5, "collision": study_collision,
+           "drag_window": study_drag_window}

@@ -1,9 +1,9 @@
 """Generate the golden vectors under tests/golden/ from the reference itself.
 
-Run in a container where the tack-lbm sources are mounted (default
-``/root/reference``, or pass the directory as the first argument):
+Run where the tack-lbm sources are available, naming their directory as the
+argument or in ``$TACK_LBM_REFERENCE``:
 
-    python tests/golden/make_golden.py [REFERENCE_DIR]
+    python tests/golden/make_golden.py REFERENCE_DIR [--only derived,...]
 
 The reference's kernels are Tack programs; ``tack_shim`` lets them execute
 as plain Python loops in float64 (the populations and fields the reference
@@ -23,6 +23,9 @@ stores as float32 are given float32 values on input). The script writes:
                       (``flutter.py``) per collision model, and ``wing_init``.
 * ``fsi_cases.npz`` - one ``fsi_step`` of the cantilever wing (``fsi.py``: moving
                       layers, interpolated bounce-back, per-layer loads).
+* ``derived_cases.npz`` - ``coarsen`` (lbm.py:516-522) and the derived fields'
+                      velocity gradient ``_jacobian`` (derived.py:52-89) on seeded
+                      output grids at strides 1, 2 and 3.
 
 Nothing reads the reference at test time; only these files are used.
 """
@@ -446,15 +449,103 @@ def make_solver_cases(ref_dir):
     np.savez_compressed(os.path.join(HERE, "solver_cases.npz"), **out)
 
 
+# (name, full lattice (nx, ny, nz), output stride, diameter): derived-field cases.
+# Odd sizes make the coarsened grid ceil(n / stride); nz = 1 and stride 3 over
+# nz = 4 give one- and two-point axes (a zero and a one-sided z derivative).
+DERIVED_CASES = [
+    ("stride1", (20, 12, 7), 1, 8.0),
+    ("stride2_odd", (21, 13, 7), 2, 8.0),
+    ("flat_z", (16, 10, 1), 1, 6.0),
+    ("stride3_thin", (17, 9, 4), 3, 12.0),
+]
+
+
+def import_derived(ref_dir):
+    """The reference derived module on the shim. It imports tack.dataset and the
+    tack-expr compiler at module level; ``_jacobian`` and ``coarsen`` use
+    neither, so empty stand-in modules let the file import."""
+    import types
+    lbm = tack_shim.import_reference(ref_dir)
+    tack = sys.modules["tack"]
+    td = types.ModuleType("tack.dataset")
+    tack.dataset = td
+    sys.modules["tack.dataset"] = td
+    sys.modules["tack_expr"] = types.ModuleType("tack_expr")
+    sys.modules.pop("derived", None)
+    import derived  # noqa: E402  (the reference module, on the shim)
+    return lbm, derived
+
+
+def derived_fields(nx, ny, nz, rng):
+    """Seeded float32 velocity fields: a developing-wake-like shear flow plus noise."""
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    ux = 0.08 * np.tanh((y - ny / 2) / 3.0) * np.cos(2 * np.pi * x / nx) + 0.05
+    uy = 0.03 * np.sin(2 * np.pi * x / nx + 0.4 * z) * np.exp(-((y - ny / 2) / 4.0) ** 2)
+    uz = 0.01 * np.cos(2 * np.pi * (x + 2 * y) / nx) * np.sin(np.pi * (z + 0.5) / max(nz, 1))
+    out = []
+    for a in (ux, uy, uz):
+        a = a + 2e-3 * rng.standard_normal(a.shape)
+        out.append(a.astype(np.float32).reshape(-1))
+    return out
+
+
+def make_derived_cases(ref_dir):
+    """The reference's own coarsen (lbm.py:516-522) and velocity gradient
+    ``_jacobian`` (derived.py:52-89, gradient="lattice") on seeded fields, with
+    inv_h = 1 / h, h = stride / diameter (derived.py:101-103)."""
+    lbm, derived = import_derived(ref_dir)
+    rng = np.random.default_rng(20241204)
+    out, meta = {}, {}
+    for name, (nx, ny, nz), stride, diameter in DERIVED_CASES:
+        t0 = time.time()
+        lat = lbm.D3Q19(nx, ny, nz)
+        full = derived_fields(nx, ny, nz, rng)
+        mx, my, mz = ((d + stride - 1) // stride for d in (nx, ny, nz))
+        m = mx * my * mz
+        coarse = []
+        for a in full:
+            dst = np.zeros(m)
+            lbm.coarsen(lat, stride, a.astype(np.float64), dst, mx, my, mz)
+            coarse.append(dst)
+        inv_h = 1.0 / (stride / diameter)
+        jac = np.zeros((m, 9))
+        derived._jacobian(coarse[0], coarse[1], coarse[2], jac, mx, my, mz, inv_h)
+        for key, a in zip(("ux", "uy", "uz"), full):
+            out[f"{name}/{key}"] = a
+        for key, a in zip(("ux", "uy", "uz"), coarse):
+            out[f"{name}/out_{key}"] = a.astype(np.float32)
+        out[f"{name}/jacobian"] = jac
+        meta[name] = dict(nx=nx, ny=ny, nz=nz, stride=stride, diameter=diameter, out_dims=[mx, my, mz],
+                          inv_h=inv_h)
+        print(f"derived {name}: {time.time() - t0:.1f} s")
+    out["meta"] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(HERE, "derived_cases.npz"), **out)
+
+
+MAKERS = {"trt_ref": make_trt_ref, "step": make_step_cases, "init": make_init_cases,
+          "solver": make_solver_cases, "heat": make_heat_cases, "wing": make_wing_cases,
+          "fsi": make_fsi_cases, "derived": make_derived_cases}
+
+
 def main():
-    ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    make_trt_ref(ref_dir)
-    make_step_cases(ref_dir)
-    make_init_cases(ref_dir)
-    make_solver_cases(ref_dir)
-    make_heat_cases(ref_dir)
-    make_wing_cases(ref_dir)
-    make_fsi_cases(ref_dir)
+    import argparse
+    ap = argparse.ArgumentParser(description="Write tests/golden/*.npz from the tack-lbm sources.")
+    ap.add_argument("reference_dir", nargs="?", default=os.environ.get("TACK_LBM_REFERENCE"),
+                    help="directory holding tack-lbm's lbm.py, trt_ref.py, flutter.py, fsi.py and "
+                         "derived.py (default: $TACK_LBM_REFERENCE)")
+    ap.add_argument("--only", default=",".join(MAKERS),
+                    help=f"comma list of the fixture sets to write (default all: {','.join(MAKERS)})")
+    args = ap.parse_args()
+    if not args.reference_dir:
+        ap.error("give the tack-lbm source directory as an argument or in $TACK_LBM_REFERENCE")
+    if not os.path.isfile(os.path.join(args.reference_dir, "lbm.py")):
+        ap.error(f"{args.reference_dir} holds no lbm.py")
+    names = [s.strip() for s in args.only.split(",") if s.strip()]
+    bad = [s for s in names if s not in MAKERS]
+    if bad:
+        ap.error(f"unknown fixture sets {bad}")
+    for name in names:
+        MAKERS[name](args.reference_dir)
 
 
 if __name__ == "__main__":

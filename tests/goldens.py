@@ -96,3 +96,13 @@ def fsi_cases():
         if m["report"]:
             case["fields"] = {k: z[f"{name}/fields/{k}"] for k in ("ux", "uy", "uz", "p", "vmag")}
         yield case
+
+
+def derived_cases():
+    """Output grids and velocity gradients from the reference's coarsen and _jacobian."""
+    z, meta = load("derived_cases")
+    for name, m in meta.items():
+        case = dict(m, name=name, full={k: z[f"{name}/{k}"] for k in ("ux", "uy", "uz")},
+                    out={k: z[f"{name}/out_{k}"] for k in ("ux", "uy", "uz")},
+                    jacobian=z[f"{name}/jacobian"])
+        yield case

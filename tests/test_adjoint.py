@@ -132,6 +132,29 @@ def test_autograd_function():
 
 
 @pytest.mark.gpu
+def test_autograd_two_applies_then_one_backward():
+    """Two losses on one run before either backward: each gradient is its own."""
+    from adjoint import DragLoss
+    run = make_run("f64")
+    p1 = torch.tensor(slice_params(), dtype=torch.float64, requires_grad=True)
+    p2 = torch.tensor(slice_params() * np.array([1.02, 1.0, 1.1, 0.97]), dtype=torch.float64,
+                      requires_grad=True)
+    l1 = DragLoss.apply(p1, run)
+    l2 = DragLoss.apply(p2, run)
+    l1.backward()
+    l2.backward()
+    ref = make_run("f64")
+    ref.forward()
+    g1 = ref.backward()
+    ref.set_params(p2.detach().numpy())
+    ref.forward()
+    g2 = ref.backward()
+    assert np.array_equal(p1.grad.numpy(), g1)
+    assert np.array_equal(p2.grad.numpy(), g2)
+    assert not np.allclose(g1, g2)
+
+
+@pytest.mark.gpu
 def test_backward_needs_current_forward():
     import lbm_native as N
     run = make_run("f32")

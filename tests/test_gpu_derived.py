@@ -1,11 +1,17 @@
 """Derived fields on the GPU (derived.py): the output grid's velocity gradient,
 vorticity and Q-criterion against the oracle, on the coarsened output grid of
-a developing cylinder flow. Tolerance: 1e-5 of the largest value (float32
-differences of float32 fields)."""
+a developing cylinder flow, and the output grid and gradient against the
+reference's own coarsen and _jacobian (golden fixtures). Tolerance: 1e-5 of
+the largest value (float32 differences of float32 fields); against the
+golden, each entry within 4 float32 roundings of its own value plus 1e-9 of
+the largest (one rounded difference, one rounded scale, float32 inv_h)."""
+
+import ctypes
 
 import numpy as np
 import pytest
 
+import goldens
 from oracle import lbm_oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -41,3 +47,28 @@ def test_derived_fields_against_oracle(stride):
         assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max(), name
     with pytest.raises(NotImplementedError):
         DerivedFields(s, {"x": ("div(velocity)", "cells")})
+
+
+@pytest.mark.parametrize("case", list(goldens.derived_cases()), ids=lambda c: c["name"])
+def test_derived_gradient_against_reference_golden(case):
+    """Fields set through the C ABI, coarsened by lbm_update_output and
+    differentiated by lbm_velocity_gradient, against the reference kernels'
+    outputs on the same fields: the output grid bit for bit, the gradient to
+    float32 rounding."""
+    import lbm
+    from derived import DerivedFields
+    s = lbm.Solver(case["nx"], case["ny"], case["nz"], collision="les", obstacle="cylinder",
+                   reynolds=100.0, u0=0.05, diameter=case["diameter"], stride=case["stride"])
+    s.sync()
+    for k, name in enumerate(("ux", "uy", "uz")):
+        v = np.ascontiguousarray(case["full"][name], np.float32)
+        s._h.call("lbm_set_field", k, v.ctypes.data_as(ctypes.c_void_p))
+    s.update_output()
+    s.sync()
+    assert tuple(s.out_dims) == tuple(case["out_dims"])
+    for name in ("ux", "uy", "uz"):
+        assert np.array_equal(s.output[name].numpy, case["out"][name]), name
+    g = DerivedFields(s).gradient().reshape(-1, 9).astype(np.float64)
+    want = case["jacobian"]
+    tol = 4 * 2.0 ** -24 * np.abs(want) + 1e-9 * np.abs(want).max()
+    assert (np.abs(g - want) <= tol).all(), np.abs(g - want).max()

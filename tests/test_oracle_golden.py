@@ -159,6 +159,19 @@ def test_velocity_gradient_of_a_linear_field():
         assert np.allclose(w, 0.4) and np.allclose(q, 0.0)
 
 
+@pytest.mark.parametrize("case", list(goldens.derived_cases()), ids=lambda c: c["name"])
+def test_derived_gradient_golden(case):
+    """The output grid and its velocity gradient against the reference's own
+    coarsen (lbm.py:516-522) and _jacobian (derived.py:52-89), run on the same
+    float32 fields: identical float64 arithmetic, so equal to the bit."""
+    dims = (case["nx"], case["ny"], case["nz"])
+    out = [O.coarsen(case["full"][k], dims, case["stride"]) for k in ("ux", "uy", "uz")]
+    for k, a in zip(("ux", "uy", "uz"), out):
+        assert np.array_equal(a, case["out"][k]), k
+    g = O.velocity_gradient(*out, tuple(case["out_dims"]), case["inv_h"]).reshape(-1, 9)
+    assert np.array_equal(g, case["jacobian"])
+
+
 @pytest.mark.parametrize("case", list(goldens.wing_cases()), ids=lambda c: c["name"])
 def test_wing_step_golden(case):
     """The pitch-plunge wing step (flutter.py:61-130) against the reference kernel."""
