@@ -272,7 +272,9 @@ lbm_status lbm_field_sums_static(const float *const fields[8], int64_t n, double
  * (ox, oy)), used wherever the reference step uses its 0/1 solid test
  * (bounce-back blend, momentum exchange, u = fluid j/rho, sponge sigma), all
  * boundaries periodic, start state lbm_init (lbm.py:383-394). Runs on its own
- * A/B population buffers in FP32 or FP64. The loss is
+ * A/B population buffers in FP32 or FP64, holding the deviations f_q - w_q
+ * from the float32 lattice weights, with the production step's pair-sum
+ * arithmetic (the stress and the density keep their digits in FP32). The loss is
  *   L = sum_{t = loss_start..steps} F_x(t) / (N_l 0.5 U^2 diameter nz),
  * F_x(t) the momentum-exchange x force of step t, N_l the number of those
  * steps. lbm_adj_backward runs the hand-written adjoint kernel backwards over
@@ -305,8 +307,9 @@ lbm_status lbm_adj_set_params(lbm_adj *h, const double par[4]);
 lbm_status lbm_adj_forward(lbm_adj *h, double *loss);
 /* dL/d(U, tau0, Cs, r) of the last forward run (synchronous). */
 lbm_status lbm_adj_backward(lbm_adj *h, double grad[4]);
-/* The state after `step` steps (a multiple of K, or 0) as 19 n values of the
- * run's precision in the layout f[q*n + idx], to a host buffer. */
+/* The state after `step` steps (a multiple of K, or 0) as 19 n values f_q of
+ * the run's precision in the layout f[q*n + idx], to a host buffer (the kept
+ * deviations plus the weights, added in that precision). */
 lbm_status lbm_adj_state(lbm_adj *h, int32_t step, void *host);
 /* {forward ms, backward ms (CUDA events), sum of F_x over the loss steps, device bytes}. */
 lbm_status lbm_adj_info(lbm_adj *h, double out[4]);

@@ -17,8 +17,18 @@
 //     which is max(here, S t^2) for a 0/1 solid.
 // The collision is LES-BGK with the Smagorinsky relaxation time of
 // lbm.py:72-93 and 126-139, every boundary is periodic, there is no rotation,
-// and the start state is lbm_init (lbm.py:383-394). All of it runs on A/B
-// buffers f[q*n + idx] in T = float or double (storage and arithmetic).
+// and the start state is lbm_init (lbm.py:383-394).
+//
+// Representation. The states are kept as deviations d_q = f_q - w_q from the
+// float32 lattice weights (the weights the reference uploads, lbm.py:48), in
+// T = float or double, on A/B buffers d[q*n + idx]; the arithmetic is the
+// production step's (lbm_device.cuh): the density from deviation pair sums,
+// the equilibrium as w_q (drho + rho (3 s + 4.5 s^2 - 1.5 u^2)) and the
+// non-equilibrium stress as pair sums minus the equilibrium's analytic second
+// moments. This is the same function of f as the plain form, but no quantity
+// of size w_q is ever subtracted from another: in float32 the stress |Pi|
+// (about 1e-5 here) keeps its digits, where the plain form loses them to the
+// rounding of f itself (4e-9 per value).
 //
 // Loss: L = 1/(N_l * 0.5 U^2 D nz) * sum over steps t = loss_start..steps of
 // F_x(t), F_x(t) the x force that step t computes from f_{t-1}.
@@ -36,6 +46,14 @@
 // transpose is a gather inside the next kernel, so one reverse step is one
 // launch. Checkpoints of f every K steps are kept by the forward run; the
 // reverse sweep recomputes each segment's states from its checkpoint.
+//
+// The obstacle band. phi is exactly zero (in T) beyond a few widths from the
+// surface. A 32 x 4 x 1 block none of whose cells or their 18 sources has
+// phi != 0 is outside the band: there g_q = p, fluid = 1, nothing bounces, no
+// force is taken and B is never touched (its entries there are zero). Such
+// blocks - most of the lattice - move 152 B per cell forward (the pull and
+// the store) and 228 B per cell in reverse (the pull, the G gather, the G
+// store); band blocks also read phi and the bounced values and write B.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -113,6 +131,7 @@ struct DArgs {
   const T *fin;
   T *fout;
   const T *phi;
+  const uint8_t *band;  // per block: 1 when a cell of the block or one of its sources has phi != 0
   const T *Bn, *Gn;  // adjoint of this step's outputs, in the B/G split
   T *Bo, *Go;        // adjoint of its inputs
   T *acc;            // per-block accumulators
@@ -146,10 +165,20 @@ __device__ __forceinline__ int shift(const Nb &o) {
          (ez == 1 ? o.zp : ez == -1 ? o.zm : 0);
 }
 
-template <typename T>
-__device__ __forceinline__ T feq1(int q, T rho, T ux, T uy, T uz, T usq) {
-  const T s = T(cx(q)) * ux + T(cy(q)) * uy + T(cz(q)) * uz;
-  return T(wq(q)) * rho * (T(1) + T(3) * s + T(4.5) * s * s - T(1.5) * usq);
+template <typename T, int q>
+__device__ __forceinline__ T cdot(T ux, T uy, T uz) {
+  T s = T(0);
+  if (cx(q)) s += T(cx(q)) * ux;
+  if (cy(q)) s += T(cy(q)) * uy;
+  if (cz(q)) s += T(cz(q)) * uz;
+  return s;
+}
+
+// feq_q - w_q = w_q (drho + rho (3 s + 4.5 s^2 - 1.5 u^2)), rho = 1 + drho
+template <typename T, int q>
+__device__ __forceinline__ T dfeq(T drho, T rho, T ux, T uy, T uz, T usq) {
+  const T s = cdot<T, q>(ux, uy, uz);
+  return T(wq(q)) * (drho + rho * (T(3) * s + T(4.5) * s * s - T(1.5) * usq));
 }
 
 // transposed Jacobian of feq(rho, u) applied to e[]: adds to rb and ub
@@ -159,15 +188,15 @@ __device__ __forceinline__ void feq_vjp(const T e[Q], T rho, T ux, T uy, T uz, T
   T a0 = 0, a1x = 0, a1y = 0, a1z = 0, a2x = 0, a2y = 0, a2z = 0, q0 = 0;
   static_for<Q>([&](auto qc) {
     constexpr int q = decltype(qc)::value;
-    const T s = T(cx(q)) * ux + T(cy(q)) * uy + T(cz(q)) * uz;
+    const T s = cdot<T, q>(ux, uy, uz);
     const T we = T(wq(q)) * e[q];
     a0 += we;
-    q0 += we * (T(1) + T(3) * s + T(4.5) * s * s);
+    q0 += we * (T(3) * s + T(4.5) * s * s);
     if (cx(q)) { a1x += T(cx(q)) * we; a2x += T(cx(q)) * we * s; }
     if (cy(q)) { a1y += T(cy(q)) * we; a2y += T(cy(q)) * we * s; }
     if (cz(q)) { a1z += T(cz(q)) * we; a2z += T(cz(q)) * we * s; }
   });
-  rb += q0 - T(1.5) * usq * a0;
+  rb += a0 + q0 - T(1.5) * usq * a0;
   ubx += rho * (T(3) * a1x + T(9) * a2x - T(3) * ux * a0);
   uby += rho * (T(3) * a1y + T(9) * a2y - T(3) * uy * a0);
   ubz += rho * (T(3) * a1z + T(9) * a2z - T(3) * uz * a0);
@@ -177,92 +206,127 @@ __device__ __forceinline__ void feq_vjp(const T e[Q], T rho, T ux, T uy, T uz, T
 template <typename T>
 struct Fwd {
   T fl, sp, sigma, keep;
-  T rho, inv, jx, jy, jz, ux, uy, uz, usq;
+  T drho, rho, inv, jx, jy, jz, ux, uy, uz, usq;
   T pi[6], pn, c, root, om;
-  T rhos, usx, usy, usz;
+  T drhos, rhos, usx, usy, usz, usqs;
 };
 
-// loads of one cell: phi at the sources, pulled and bounced values, streamed g
+// Moments, stress, relaxation time and sponge of one cell from its streamed
+// deviations g[] (the production step's pair arithmetic, lbm_device.cuh).
 template <typename T>
-__device__ __forceinline__ void load_cell(const DArgs<T> &a, int idx, const Nb &o, T ph[Q], T p[Q], T b[Q],
-                                          T g[Q]) {
-  static_for<Q>([&](auto qc) {
-    constexpr int q = decltype(qc)::value;
-    const int s = idx + shift<q, -1>(o);
-    ph[q] = a.phi[s];
-    p[q] = a.fin[(size_t)q * a.n + s];
-    b[q] = a.fin[(size_t)opp(q) * a.n + idx];
-    g[q] = q == 0 ? p[q] : p[q] + ph[q] * (b[q] - p[q]);
-  });
-}
-
-template <typename T>
-__device__ __forceinline__ void forward_cell(const DArgs<T> &a, int x, T phix, const T g[Q], Fwd<T> &F) {
-  F.fl = T(1) - phix;
-  T rho = 0, jx = 0, jy = 0, jz = 0;
-  static_for<Q>([&](auto qc) {
-    constexpr int q = decltype(qc)::value;
-    rho += g[q];
-    if (cx(q)) jx += T(cx(q)) * g[q];
-    if (cy(q)) jy += T(cy(q)) * g[q];
-    if (cz(q)) jz += T(cz(q)) * g[q];
-  });
-  F.rho = rho;
-  F.inv = T(1) / rho;
-  F.jx = jx;
-  F.jy = jy;
-  F.jz = jz;
-  F.ux = F.fl * jx * F.inv;
-  F.uy = F.fl * jy * F.inv;
-  F.uz = F.fl * jz * F.inv;
-  F.usq = F.ux * F.ux + F.uy * F.uy + F.uz * F.uz;
-  T pxx = 0, pyy = 0, pzz = 0, pxy = 0, pxz = 0, pyz = 0;
-  static_for<Q>([&](auto qc) {
-    constexpr int q = decltype(qc)::value;
-    const T ne = g[q] - feq1<T>(q, F.rho, F.ux, F.uy, F.uz, F.usq);
-    if (cx(q)) pxx += ne;
-    if (cy(q)) pyy += ne;
-    if (cz(q)) pzz += ne;
-    if (cx(q) && cy(q)) pxy += T(cx(q) * cy(q)) * ne;
-    if (cx(q) && cz(q)) pxz += T(cx(q) * cz(q)) * ne;
-    if (cy(q) && cz(q)) pyz += T(cy(q) * cz(q)) * ne;
-  });
-  F.pi[0] = pxx; F.pi[1] = pyy; F.pi[2] = pzz; F.pi[3] = pxy; F.pi[4] = pxz; F.pi[5] = pyz;
-  F.pn = sqrt(pxx * pxx + pyy * pyy + pzz * pzz + T(2) * (pxy * pxy + pxz * pxz + pyz * pyz));
+__device__ __forceinline__ void forward_cell(const DArgs<T> &a, int x, T fl, const T g[Q], Fwd<T> &F) {
+  T D[9], M[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    D[k] = g[pq(k)] + g[pq(k) + 1];
+    M[k] = g[pq(k)] - g[pq(k) + 1];
+  }
+  T sum = g[0];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) sum += D[k];
+  F.fl = fl;
+  F.drho = sum + T(W_EXCESS);
+  F.rho = T(1) + F.drho;
+  F.inv = T(1) / F.rho;
+  F.jx = M[0] + M[3] + M[4] + M[5] + M[6];
+  F.jy = M[1] + M[3] - M[4] + M[7] + M[8];
+  F.jz = M[2] + M[5] - M[6] + M[7] - M[8];
+  F.ux = fl * F.jx * F.inv;
+  F.uy = fl * F.jy * F.inv;
+  F.uz = fl * F.jz * F.inv;
+  const T uxx = F.ux * F.ux, uyy = F.uy * F.uy, uzz = F.uz * F.uz;
+  F.usq = uxx + uyy + uzz;
+  // Pi_ab = sum c_a c_b (g - feq): deviation pair sums minus the equilibrium's
+  // second moments, W2 (drho - 1.5 rho u^2) + 4.5 rho (W2 u_a^2 + W22 (u^2 - u_a^2))
+  // on the diagonal and 9 rho W22 u_a u_b off it (lbm_device.cuh, collide())
+  const T r45 = T(4.5) * F.rho;
+  const T iso = T(W2) * (F.drho - T(1.5) * F.rho * F.usq) + r45 * T(W22) * F.usq;
+  const T diag = r45 * T(W2 - W22);
+  const T offd = T(9) * F.rho * T(W22);
+  F.pi[0] = (D[0] + D[3] + D[4] + D[5] + D[6]) - iso - diag * uxx;
+  F.pi[1] = (D[1] + D[3] + D[4] + D[7] + D[8]) - iso - diag * uyy;
+  F.pi[2] = (D[2] + D[5] + D[6] + D[7] + D[8]) - iso - diag * uzz;
+  F.pi[3] = (D[3] - D[4]) - offd * F.ux * F.uy;
+  F.pi[4] = (D[5] - D[6]) - offd * F.ux * F.uz;
+  F.pi[5] = (D[7] - D[8]) - offd * F.uy * F.uz;
+  F.pn = sqrt(F.pi[0] * F.pi[0] + F.pi[1] * F.pi[1] + F.pi[2] * F.pi[2] +
+              T(2) * (F.pi[3] * F.pi[3] + F.pi[4] * F.pi[4] + F.pi[5] * F.pi[5]));
   F.c = T(SMAG) * a.cs * a.cs;
   F.root = sqrt(a.tau0 * a.tau0 + F.c * F.pn * F.inv);
   F.om = T(1) / (T(0.5) * (a.tau0 + F.root));
   const T t = fmax(T(0), (T(x) - a.sponge_start) * a.inv_sponge_len);
   F.sp = a.sponge_strength * t * t;
-  F.sigma = T(1) - F.fl * (T(1) - F.sp);
+  F.sigma = T(1) - fl * (T(1) - F.sp);
   F.keep = T(1) - F.sigma;
-  F.rhos = F.rho + F.sigma * (T(1) - F.rho);
-  F.usx = F.ux + F.sigma * (a.u0 * F.fl - F.ux);
+  // rho_s = rho + sigma (1 - rho) = 1 + keep drho
+  F.drhos = F.keep * F.drho;
+  F.rhos = T(1) + F.drhos;
+  F.usx = F.ux + F.sigma * (a.u0 * fl - F.ux);
   F.usy = F.keep * F.uy;
   F.usz = F.keep * F.uz;
+  F.usqs = F.usx * F.usx + F.usy * F.usy + F.usz * F.usz;
+}
+
+// Streamed deviations g[] of cell idx. BAND: the bounce-back blend with phi at
+// the sources; otherwise the plain pull.
+template <typename T, bool BAND>
+__device__ __forceinline__ void stream_cell(const DArgs<T> &a, int idx, const Nb &o, T g[Q]) {
+  static_for<Q>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    const int s = idx + shift<q, -1>(o);
+    const T p = __ldg(a.fin + q * a.n + s);
+    if (BAND && q != 0) {
+      const T ph = __ldg(a.phi + s);
+      const T b = __ldg(a.fin + opp(q) * a.n + idx);
+      g[q] = p + ph * (b - p);
+    } else {
+      g[q] = p;
+    }
+  });
+}
+
+// x force of one band cell from its bounced values: sum_q -c_qx phi_q fl 2 (w + b)
+template <typename T>
+__device__ __forceinline__ T cell_force(const DArgs<T> &a, int idx, const Nb &o, T fl) {
+  T force = T(0);
+  static_for<Q>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    if (q != 0 && cx(q) != 0) {
+      const T ph = __ldg(a.phi + idx + shift<q, -1>(o));
+      const T b = __ldg(a.fin + opp(q) * a.n + idx);
+      force += T(-cx(q)) * ph * fl * T(2) * (T(wq(q)) + b);
+    }
+  });
+  return force;
+}
+
+template <typename T, bool BAND>
+__device__ __forceinline__ T step_cell(const DArgs<T> &a, int x, int idx, const Nb &o) {
+  T g[Q];
+  stream_cell<T, BAND>(a, idx, o, g);
+  const T fl = BAND ? T(1) - __ldg(a.phi + idx) : T(1);
+  Fwd<T> F;
+  forward_cell(a, x, fl, g, F);
+  // out = feq(rho_s, u_s) + keep (post - feq) = feq_s + keep (1 - om) (g - feq)
+  const T alpha = F.keep * (T(1) - F.om);
+  static_for<Q>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    const T ne = g[q] - dfeq<T, q>(F.drho, F.rho, F.ux, F.uy, F.uz, F.usq);
+    a.fout[q * a.n + idx] = dfeq<T, q>(F.drhos, F.rhos, F.usx, F.usy, F.usz, F.usqs) + alpha * ne;
+  });
+  return BAND && a.beta != T(0) ? cell_force(a, idx, o, fl) : T(0);
 }
 
 // Forward step f_{t-1} -> f_t; when beta != 0 also the step's x force.
 template <typename T>
 __global__ void __launch_bounds__(BX * BY) diff_step_kernel(const __grid_constant__ DArgs<T> a) {
   const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
+  const bool band = a.band[block_id()] != 0;
   T force = 0;
   if (x < a.nx && y < a.ny) {
     const int idx = (z * a.ny + y) * a.nx + x;
     const Nb o = neighbours(x, y, z, a.nx, a.ny, a.nz);
-    T ph[Q], p[Q], b[Q], g[Q];
-    load_cell(a, idx, o, ph, p, b, g);
-    Fwd<T> F;
-    forward_cell(a, x, ph[0], g, F);
-    const T usq_s = F.usx * F.usx + F.usy * F.usy + F.usz * F.usz;
-    static_for<Q>([&](auto qc) {
-      constexpr int q = decltype(qc)::value;
-      const T e0 = feq1<T>(q, F.rho, F.ux, F.uy, F.uz, F.usq);
-      const T post = g[q] + F.om * (e0 - g[q]);
-      const T e1 = feq1<T>(q, F.rhos, F.usx, F.usy, F.usz, usq_s);
-      a.fout[(size_t)q * a.n + idx] = e1 + F.keep * (post - e0);
-      if (q != 0 && cx(q) != 0) force += T(-cx(q)) * ph[q] * F.fl * T(2) * b[q];
-    });
+    force = band ? step_cell<T, true>(a, x, idx, o) : step_cell<T, false>(a, x, idx, o);
   }
   if (a.beta != T(0)) {
     T v[1] = {force};
@@ -270,103 +334,125 @@ __global__ void __launch_bounds__(BX * BY) diff_step_kernel(const __grid_constan
   }
 }
 
-// Reverse of step t: lambda_t (B/G split) -> lambda_{t-1} (B/G split) and the
-// parameter gradients of the step.
+// Reverse of step t for one cell: lambda_t (B/G split) -> lambda_{t-1} (B/G
+// split) and the cell's parameter gradients.
+template <typename T, bool BAND>
+__device__ __forceinline__ void adjoint_cell(const DArgs<T> &a, int x, int idx, const Nb &o, T grad[NPAR]) {
+  T g[Q];
+  stream_cell<T, BAND>(a, idx, o, g);
+  const T phx = BAND ? __ldg(a.phi + idx) : T(0);
+  Fwd<T> F;
+  forward_cell(a, x, T(1) - phx, g, F);
+  // g <- ne = g - feq(rho, u)
+  static_for<Q>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    g[q] -= dfeq<T, q>(F.drho, F.rho, F.ux, F.uy, F.uz, F.usq);
+  });
+  // adjoint of the outputs f_t[q](x)
+  T ob[Q];
+  static_for<Q>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    const T gin = a.Gn[q * a.n + idx + shift<q, 1>(o)];
+    ob[q] = (BAND && q != 0) ? a.Bn[q * a.n + idx] + gin : gin;
+  });
+  // out = feq(rho_s, u_s) + keep (1 - om) ne
+  T rsb = 0, usbx = 0, usby = 0, usbz = 0;
+  feq_vjp<T>(ob, F.rhos, F.usx, F.usy, F.usz, rsb, usbx, usby, usbz);
+  T s1 = 0;  // sum ob ne
+  static_for<Q>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    s1 += ob[q] * g[q];
+  });
+  const T one_om = T(1) - F.om;
+  const T alpha = F.keep * one_om;
+  const T kb = one_om * s1;     // d/d keep
+  const T omb = -F.keep * s1;   // d/d om
+  // sponge blend: rho_s, u_s, keep = 1 - sigma
+  T sigb = -kb - rsb * F.drho + usbx * (a.u0 * F.fl - F.ux) - usby * F.uy - usbz * F.uz;
+  T rhob = rsb * F.keep;
+  T uxb = usbx * F.keep, uyb = usby * F.keep, uzb = usbz * F.keep;
+  grad[0] += usbx * F.sigma * F.fl;
+  T flb = usbx * F.sigma * a.u0 - sigb * (T(1) - F.sp);
+  // om = 1/tau, tau = (tau0 + root)/2, root^2 = tau0^2 + c pn / rho
+  const T taub = -omb * F.om * F.om;
+  const T innerb = taub / (T(4) * F.root);
+  grad[1] += T(0.5) * taub + innerb * T(2) * a.tau0;
+  grad[2] += innerb * F.pn * F.inv * T(SMAG) * T(2) * a.cs;
+  const T pnb = innerb * F.c * F.inv;
+  rhob -= innerb * F.c * F.pn * F.inv * F.inv;
+  T pib[6] = {0, 0, 0, 0, 0, 0};
+  if (F.pn > T(0)) {
+    const T s = pnb / F.pn;
+    pib[0] = s * F.pi[0];
+    pib[1] = s * F.pi[1];
+    pib[2] = s * F.pi[2];
+    pib[3] = T(2) * s * F.pi[3];
+    pib[4] = T(2) * s * F.pi[4];
+    pib[5] = T(2) * s * F.pi[5];
+  }
+  // ne = g - feq: gb = alpha ob + sum_ab c_a c_b pib_ab, and feq's adjoint is -gb
+  static_for<Q>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    T m = 0;
+    if (cx(q)) m += pib[0];
+    if (cy(q)) m += pib[1];
+    if (cz(q)) m += pib[2];
+    if (cx(q) && cy(q)) m += T(cx(q) * cy(q)) * pib[3];
+    if (cx(q) && cz(q)) m += T(cx(q) * cz(q)) * pib[4];
+    if (cy(q) && cz(q)) m += T(cy(q) * cz(q)) * pib[5];
+    ob[q] = alpha * ob[q] + m;
+  });
+  {
+    T r = 0, bx = 0, by = 0, bz = 0;
+    feq_vjp<T>(ob, F.rho, F.ux, F.uy, F.uz, r, bx, by, bz);
+    rhob -= r;
+    uxb -= bx;
+    uyb -= by;
+    uzb -= bz;
+  }
+  // u = fl j / rho
+  const T jxb = uxb * F.fl * F.inv, jyb = uyb * F.fl * F.inv, jzb = uzb * F.fl * F.inv;
+  rhob -= (uxb * F.ux + uyb * F.uy + uzb * F.uz) * F.inv;
+  flb += (uxb * F.jx + uyb * F.jy + uzb * F.jz) * F.inv;
+  // moments, streaming and bounce-back (and the drag); outputs
+  T rb = 0;
+  static_for<Q>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    const T gq = ob[q] + rhob + T(cx(q)) * jxb + T(cy(q)) * jyb + T(cz(q)) * jzb;
+    if (!BAND || q == 0) {
+      a.Go[q * a.n + idx] = gq;
+    } else {
+      const int s = idx + shift<q, -1>(o);
+      const T ph = __ldg(a.phi + s);
+      const T b = __ldg(a.fin + opp(q) * a.n + idx);
+      const T p = __ldg(a.fin + q * a.n + s);
+      T bb = gq * ph;
+      T phb = gq * (b - p);
+      if (cx(q) != 0 && a.beta != T(0)) {
+        const T d = a.beta * T(-cx(q)) * T(2);
+        const T bf = T(wq(q)) + b;  // the bounced population itself
+        bb += d * ph * F.fl;
+        phb += d * F.fl * bf;
+        flb += d * ph * bf;
+      }
+      a.Go[q * a.n + idx] = gq * (T(1) - ph);
+      a.Bo[opp(q) * a.n + idx] = bb;
+      rb += phb * T(2) * ph * (T(1) - ph) * a.inv_width;
+    }
+  });
+  if (BAND) grad[3] += rb - flb * T(2) * phx * (T(1) - phx) * a.inv_width;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(BX * BY) diff_adjoint_kernel(const __grid_constant__ DArgs<T> a) {
   const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
+  const bool band = a.band[block_id()] != 0;
   T grad[NPAR] = {0, 0, 0, 0};
   if (x < a.nx && y < a.ny) {
     const int idx = (z * a.ny + y) * a.nx + x;
     const Nb o = neighbours(x, y, z, a.nx, a.ny, a.nz);
-    T ph[Q], p[Q], b[Q], g[Q];
-    load_cell(a, idx, o, ph, p, b, g);
-    Fwd<T> F;
-    forward_cell(a, x, ph[0], g, F);
-    // adjoint of the outputs f_t[q](x)
-    T ob[Q];
-    static_for<Q>([&](auto qc) {
-      constexpr int q = decltype(qc)::value;
-      ob[q] = a.Bn[(size_t)q * a.n + idx] + a.Gn[(size_t)q * a.n + idx + shift<q, 1>(o)];
-    });
-    // out = feq(rhos, us) + keep (post - feq(rho, u))
-    T rsb = 0, usbx = 0, usby = 0, usbz = 0;
-    feq_vjp<T>(ob, F.rhos, F.usx, F.usy, F.usz, rsb, usbx, usby, usbz);
-    T kb = 0, omb = 0, e0b[Q], gb[Q];
-    static_for<Q>([&](auto qc) {
-      constexpr int q = decltype(qc)::value;
-      const T e0 = feq1<T>(q, F.rho, F.ux, F.uy, F.uz, F.usq);
-      const T post = g[q] + F.om * (e0 - g[q]);
-      kb += ob[q] * (post - e0);
-      const T pb = F.keep * ob[q];
-      gb[q] = (T(1) - F.om) * pb;
-      e0b[q] = -F.keep * ob[q] + F.om * pb;
-      omb += pb * (e0 - g[q]);
-    });
-    // sponge blend: rhos, us, keep = 1 - sigma
-    T sigb = -kb + rsb * (T(1) - F.rho) + usbx * (a.u0 * F.fl - F.ux) - usby * F.uy - usbz * F.uz;
-    T rhob = rsb * F.keep;
-    T uxb = usbx * F.keep, uyb = usby * F.keep, uzb = usbz * F.keep;
-    grad[0] += usbx * F.sigma * F.fl;
-    T flb = usbx * F.sigma * a.u0 - sigb * (T(1) - F.sp);
-    // om = 1/tau, tau = (tau0 + root)/2, root^2 = tau0^2 + c pn / rho
-    const T taub = -omb * F.om * F.om;
-    const T innerb = taub / (T(4) * F.root);
-    grad[1] += T(0.5) * taub + innerb * T(2) * a.tau0;
-    grad[2] += innerb * F.pn * F.inv * T(SMAG) * T(2) * a.cs;
-    const T pnb = innerb * F.c * F.inv;
-    rhob -= innerb * F.c * F.pn * F.inv * F.inv;
-    T pib[6] = {0, 0, 0, 0, 0, 0};
-    if (F.pn > T(0)) {
-      const T s = pnb / F.pn;
-      pib[0] = s * F.pi[0];
-      pib[1] = s * F.pi[1];
-      pib[2] = s * F.pi[2];
-      pib[3] = T(2) * s * F.pi[3];
-      pib[4] = T(2) * s * F.pi[4];
-      pib[5] = T(2) * s * F.pi[5];
-    }
-    static_for<Q>([&](auto qc) {
-      constexpr int q = decltype(qc)::value;
-      T m = 0;
-      if (cx(q)) m += pib[0];
-      if (cy(q)) m += pib[1];
-      if (cz(q)) m += pib[2];
-      if (cx(q) && cy(q)) m += T(cx(q) * cy(q)) * pib[3];
-      if (cx(q) && cz(q)) m += T(cx(q) * cz(q)) * pib[4];
-      if (cy(q) && cz(q)) m += T(cy(q) * cz(q)) * pib[5];
-      gb[q] += m;
-      e0b[q] -= m;
-    });
-    feq_vjp<T>(e0b, F.rho, F.ux, F.uy, F.uz, rhob, uxb, uyb, uzb);
-    // u = fl j / rho
-    const T jxb = uxb * F.fl * F.inv, jyb = uyb * F.fl * F.inv, jzb = uzb * F.fl * F.inv;
-    rhob -= (uxb * F.ux + uyb * F.uy + uzb * F.uz) * F.inv;
-    flb += (uxb * F.jx + uyb * F.jy + uzb * F.jz) * F.inv;
-    // drag, streaming and bounce-back; outputs
-    const T dphx = T(2) * ph[0] * (T(1) - ph[0]) * a.inv_width;
-    T rb = 0;
-    a.Bo[idx] = T(0);
-    static_for<Q>([&](auto qc) {
-      constexpr int q = decltype(qc)::value;
-      T gq = gb[q] + rhob + T(cx(q)) * jxb + T(cy(q)) * jyb + T(cz(q)) * jzb;
-      if (q == 0) {
-        a.Go[idx] = gq;
-      } else {
-        T bb = gq * ph[q];
-        T phb = gq * (b[q] - p[q]);
-        if (cx(q) != 0 && a.beta != T(0)) {
-          const T d = a.beta * T(-cx(q)) * T(2);
-          bb += d * ph[q] * F.fl;
-          phb += d * F.fl * b[q];
-          flb += d * ph[q] * b[q];
-        }
-        a.Go[(size_t)q * a.n + idx] = gq * (T(1) - ph[q]);
-        a.Bo[(size_t)opp(q) * a.n + idx] = bb;
-        rb += phb * T(2) * ph[q] * (T(1) - ph[q]) * a.inv_width;
-      }
-    });
-    grad[3] += rb - flb * dphx;
+    if (band) adjoint_cell<T, true>(a, x, idx, o, grad);
+    else adjoint_cell<T, false>(a, x, idx, o, grad);
   }
   block_accumulate<T, NPAR>(grad, a.acc);
 }
@@ -389,7 +475,7 @@ __global__ void diff_init_kernel(const __grid_constant__ DArgs<T> a) {
     const T usq = ux * ux + uy * uy;
     static_for<Q>([&](auto qc) {
       constexpr int q = decltype(qc)::value;
-      a.fout[(size_t)q * a.n + idx] = feq1<T>(q, T(1), ux, uy, T(0), usq);
+      a.fout[q * a.n + idx] = dfeq<T, q>(T(0), T(1), ux, uy, T(0), usq);
     });
   }
 }
@@ -398,6 +484,7 @@ __global__ void diff_init_kernel(const __grid_constant__ DArgs<T> a) {
 template <typename T>
 __global__ void __launch_bounds__(BX * BY) diff_init_adjoint_kernel(const __grid_constant__ DArgs<T> a) {
   const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
+  const bool band = a.band[block_id()] != 0;
   T grad[NPAR] = {0, 0, 0, 0};
   if (x < a.nx && y < a.ny) {
     const int idx = (z * a.ny + y) * a.nx + x;
@@ -405,7 +492,8 @@ __global__ void __launch_bounds__(BX * BY) diff_init_adjoint_kernel(const __grid
     T e[Q];
     static_for<Q>([&](auto qc) {
       constexpr int q = decltype(qc)::value;
-      e[q] = a.Bn[(size_t)q * a.n + idx] + a.Gn[(size_t)q * a.n + idx + shift<q, 1>(o)];
+      const T gin = a.Gn[q * a.n + idx + shift<q, 1>(o)];
+      e[q] = (band && q != 0) ? a.Bn[q * a.n + idx] + gin : gin;
     });
     const T phx = a.phi[idx], fl = T(1) - phx;
     T ux, uy, wave;
@@ -428,6 +516,29 @@ __global__ void phi_kernel(T *phi, int nx, int ny, int n, T ox, T oy, T r, T inv
   }
 }
 
+// Band flags: a cell with phi != 0 marks its own block and the blocks of the
+// 18 cells that pull from it (x + c_q, periodic). Every flag written is 1, so
+// the concurrent stores need no atomics.
+template <typename T>
+__global__ void band_kernel(const T *phi, uint8_t *band, int nx, int ny, int nz, int gx, int gy) {
+  const int n = nx * ny * nz;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    if (phi[idx] == T(0)) continue;
+    const int x = idx % nx, y = (idx / nx) % ny, z = idx / (nx * ny);
+    static_for<Q>([&](auto qc) {
+      constexpr int q = decltype(qc)::value;
+      int xs = x + cx(q), ys = y + cy(q), zs = z + cz(q);
+      xs += xs < 0 ? nx : 0;
+      xs -= xs >= nx ? nx : 0;
+      ys += ys < 0 ? ny : 0;
+      ys -= ys >= ny ? ny : 0;
+      zs += zs < 0 ? nz : 0;
+      zs -= zs >= nz ? nz : 0;
+      band[((size_t)zs * gy + ys / BY) * gx + xs / BX] = 1;
+    });
+  }
+}
+
 }  // namespace lbma
 
 // ---------------------------------------------------------------------------
@@ -440,6 +551,7 @@ struct lbm_adj {
   size_t esz;        // bytes per value (4 or 8)
   size_t state;      // bytes per population state (19 n values)
   void *phi = nullptr;
+  uint8_t *band = nullptr;  // per-block obstacle-band flags
   std::vector<void *> ck;   // checkpoints f_{mK}, m = 0..M
   std::vector<void *> seg;  // recomputed states of one segment
   void *tmp[2] = {nullptr, nullptr};
@@ -475,6 +587,7 @@ lbma::DArgs<T> dargs(const lbm_adj *h) {
   lbma::DArgs<T> a{};
   const lbm_adj_config &c = h->cfg;
   a.phi = static_cast<const T *>(h->phi);
+  a.band = h->band;
   a.nx = c.nx;
   a.ny = c.ny;
   a.nz = c.nz;
@@ -518,6 +631,9 @@ lbm_status phi_and_init(lbm_adj *h, void *f0) {
   const int g = lbmk::cell_grid(h->n);
   lbma::phi_kernel<T><<<g, 256>>>(static_cast<T *>(h->phi), c.nx, c.ny, (int)h->n, (T)c.ox, (T)c.oy,
                                   (T)h->par[3], (T)(1.0 / c.width));
+  ACUDA(cudaMemsetAsync(h->band, 0, (size_t)h->nblocks));
+  lbma::band_kernel<T><<<g, 256>>>(static_cast<const T *>(h->phi), h->band, c.nx, c.ny, c.nz, (int)h->grid.x,
+                                   (int)h->grid.y);
   lbma::DArgs<T> a = dargs<T>(h);
   a.fout = static_cast<T *>(f0);
   lbma::diff_init_kernel<T><<<g, 256>>>(a);
@@ -613,6 +729,7 @@ lbm_status backward(lbm_adj *h, double grad[4]) {
 
 void release(lbm_adj *h) {
   cudaFree(h->phi);
+  cudaFree(h->band);
   for (void *p : h->ck) cudaFree(p);
   for (size_t i = 1; i < h->seg.size(); ++i) cudaFree(h->seg[i]);
   for (void *&p : h->tmp) cudaFree(p);
@@ -658,6 +775,7 @@ lbm_status lbm_adj_create(const lbm_adj_config *cfg, lbm_adj **out) {
     return e;
   };
   cudaError_t e = alloc(&h->phi, (size_t)h->n * h->esz);
+  if (e == cudaSuccess) e = alloc((void **)&h->band, (size_t)h->nblocks);
   h->ck.assign(M + 1, nullptr);
   for (int m = 0; m <= M && e == cudaSuccess; ++m) e = alloc(&h->ck[m], h->state);
   h->seg.assign(c.checkpoint, nullptr);
@@ -717,6 +835,17 @@ lbm_status lbm_adj_state(lbm_adj *h, int32_t step, void *host) {
     return afail(LBM_ERR_ARG, "step must be a checkpointed step (a multiple of the checkpoint interval)");
   ACUDA(cudaSetDevice(h->cfg.device));
   ACUDA(cudaMemcpy(host, h->ck[step / h->cfg.checkpoint], h->state, cudaMemcpyDeviceToHost));
+  // the run keeps deviations f_q - w_q: add the weights back
+  const int64_t n = h->n;
+  for (int q = 0; q < lbmk::Q; ++q) {
+    if (h->cfg.precision == LBM_F64) {
+      double *f = static_cast<double *>(host) + (size_t)q * n;
+      for (int64_t i = 0; i < n; ++i) f[i] += (double)lbmk::wq(q);
+    } else {
+      float *f = static_cast<float *>(host) + (size_t)q * n;
+      for (int64_t i = 0; i < n; ++i) f[i] += lbmk::wq(q);
+    }
+  }
   return LBM_OK;
 }
 

@@ -8,8 +8,13 @@ Tolerances:
 * FP64 adjoint vs central differences of the FP64 forward run, step 1e-3 of
   each parameter: 1e-4 relative (the differences' own truncation error is
   ~1e-6 here);
-* FP32 adjoint vs the FP64 adjoint: 2e-3 relative, the accumulated float32
-  round-off of the forward and reverse sweeps.
+* FP32 adjoint vs the FP64 adjoint: 1e-5 relative on the slice (measured
+  5.5e-7), the accumulated float32 round-off of the forward and reverse
+  sweeps over deviations f - w;
+* at full size (256 x 128 x 32, 2000 steps): the FP32 and the FP64 adjoint
+  both within 1e-4 of FP64 central differences (measured 4.1e-6, the
+  differences' own truncation error), and within 2e-5 of each other
+  (measured 1.5e-6).
 """
 
 import numpy as np
@@ -103,8 +108,8 @@ def test_fp32_adjoint_against_fp64():
     r64, r32 = make_run("f64"), make_run("f32")
     l64, l32 = r64.forward(), r32.forward()
     g64, g32 = r64.backward(), r32.backward()
-    assert rel_err(l32, l64) < 1e-4
-    assert rel_err(g32, g64).max() < 2e-3, (g32, g64)
+    assert rel_err(l32, l64) < 1e-6
+    assert rel_err(g32, g64).max() < 1e-5, (g32, g64)
 
 
 @pytest.mark.gpu
@@ -168,11 +173,11 @@ def test_backward_needs_current_forward():
 
 @pytest.mark.gpu
 @pytest.mark.slow
-def test_full_size_fp64_adjoint_matches_central_differences():
+def test_full_size_adjoint_matches_central_differences():
     """256 x 128 x 32 LES cylinder at Re 100, 2000 steps, loss over steps
     1001..2000, checkpoints every 100 steps; r = 8, width 1.5, U = 0.05, Cs = 0.1.
-    The FP64 adjoint against FP64 central differences (h = 1e-3 relative), and
-    the FP32 adjoint against the FP64 one."""
+    The FP64 and the FP32 adjoint against FP64 central differences
+    (h = 1e-3 relative): 1e-4, the gradient tolerance the adjoint is held to."""
     from adjoint import DragAdjoint
     kw = dict(steps=2000, loss_start=1001, checkpoint=100, u0=0.05, reynolds=100.0, cs=0.1, r=8.0,
               width=1.5)
@@ -196,4 +201,5 @@ def test_full_size_fp64_adjoint_matches_central_differences():
     r32 = DragAdjoint(256, 128, 32, precision="f32", **kw)
     r32.forward()
     g32 = r32.backward()
-    assert rel_err(g32, g64).max() < 1e-2, (g32, g64)
+    assert rel_err(g32, fd).max() < 1e-4, (g32, fd)
+    assert rel_err(g32, g64).max() < 2e-5, (g32, g64)
