@@ -242,8 +242,18 @@ lbm_status lbm_timing_read(lbm_solver *s, double out[7]);
  * (synchronous). (No reference counterpart: measurement support.) */
 lbm_status lbm_run_timed(lbm_solver *s, int32_t count, int32_t report_last, void *stream, double *ms);
 
-/* Synchronise the solver's device work (tack.sync, lbm.py:651). */
+/* Synchronise the solver's device work (tack.sync, lbm.py:651). Returns
+ * LBM_ERR_CUDA when a bulk-copy step gave up waiting for its copies since the
+ * last check (the populations are then invalid), and clears that state. */
 lbm_status lbm_sync(lbm_solver *s);
+
+/* Test hook of the bulk-copy kernel's bounded waits (LBM_FLAG_BULKCOPY): the
+ * next lbm_step issues no copies, so every wait of its consumers runs out
+ * after wait_polls polls. Nothing is read or written in HBM by that step; the
+ * next lbm_sync returns LBM_ERR_CUDA. LBM_ERR_STATE for a solver without the
+ * bulk-copy kernel; lbm_run refuses to run while the hook is pending.
+ * (No reference counterpart: failure-path testing.) */
+lbm_status lbm_test_bulkcopy_stall(lbm_solver *s, int64_t wait_polls);
 
 /* Largest n accepted by lbm_field_sums_static: 2^28 cells. */
 #define LBM_STATIC_SUMS_MAX_CELLS 268435456LL

@@ -72,6 +72,23 @@ namespace lbma {
 using namespace lbmk;
 
 constexpr int NPAR = 4;  // U, tau0, Cs, r
+
+// Resident blocks per SM of the forward and reverse kernels in float32 (the
+// timed precision); float64 leaves the register count to the compiler.
+#ifndef LBM_ADJ_STEP_MIN_BLOCKS
+#define LBM_ADJ_STEP_MIN_BLOCKS 5
+#endif
+#ifndef LBM_ADJ_REVERSE_MIN_BLOCKS
+#define LBM_ADJ_REVERSE_MIN_BLOCKS 3
+#endif
+template <typename T>
+constexpr int adj_step_blocks() {
+  return sizeof(T) == 4 ? LBM_ADJ_STEP_MIN_BLOCKS : 1;
+}
+template <typename T>
+constexpr int adj_reverse_blocks() {
+  return sizeof(T) == 4 ? LBM_ADJ_REVERSE_MIN_BLOCKS : 1;
+}
 constexpr double SMAG = 25.456;  // 18 sqrt(2) as the reference writes it (lbm.py:93)
 
 template <typename T> __device__ __forceinline__ T add_rn(T a, T b);
@@ -319,7 +336,7 @@ __device__ __forceinline__ T step_cell(const DArgs<T> &a, int x, int idx, const 
 
 // Forward step f_{t-1} -> f_t; when beta != 0 also the step's x force.
 template <typename T>
-__global__ void __launch_bounds__(BX * BY) diff_step_kernel(const __grid_constant__ DArgs<T> a) {
+__global__ void __launch_bounds__(BX * BY, adj_step_blocks<T>()) diff_step_kernel(const __grid_constant__ DArgs<T> a) {
   const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
   const bool band = a.band[block_id()] != 0;
   T force = 0;
@@ -444,7 +461,8 @@ __device__ __forceinline__ void adjoint_cell(const DArgs<T> &a, int x, int idx, 
 }
 
 template <typename T>
-__global__ void __launch_bounds__(BX * BY) diff_adjoint_kernel(const __grid_constant__ DArgs<T> a) {
+__global__ void __launch_bounds__(BX * BY, adj_reverse_blocks<T>())
+diff_adjoint_kernel(const __grid_constant__ DArgs<T> a) {
   const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
   const bool band = a.band[block_id()] != 0;
   T grad[NPAR] = {0, 0, 0, 0};

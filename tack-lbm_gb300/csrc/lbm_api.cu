@@ -449,6 +449,8 @@ lbm_status lbm_create(const lbm_config *cfg, lbm_solver **out) {
     const int tail = cfg->nx % lbmk::SW;
     c.use_stream = (cfg->flags & LBM_FLAG_BULKCOPY) && !(cfg->flags & LBM_FLAG_SIMT) && !cfg->heat && cfg->nx % h == 0 &&
                    cfg->nx >= 2 * h && (tail == 0 || tail >= 2 * h);
+    c.wait_limit = lbmk::WAIT_LIMIT;
+    c.starve_next = 0;
     c.nseg_x = (cfg->nx + lbmk::SW - 1) / lbmk::SW;
     c.nseg = c.nseg_x * cfg->ny * cfg->nz;
   }
@@ -569,7 +571,12 @@ lbm_status lbm_init_random(lbm_solver *s, double rho_sigma, double u_noise, uint
 lbm_status lbm_step(lbm_solver *s, int32_t report, void *stream) {
   lbmh::Range range_("lbm_step");
   LBM_HANDLE(s);
-  LBM_CUDA(dispatch_step(s->c, report != 0, (cudaStream_t)stream));
+  const cudaError_t es = dispatch_step(s->c, report != 0, (cudaStream_t)stream);
+  if (s->c.starve_next) {  // the stall test hook covers one step
+    s->c.starve_next = 0;
+    s->c.wait_limit = lbmk::WAIT_LIMIT;
+  }
+  LBM_CUDA(es);
   if (s->c.cfg.heat) {
     LBM_CUDA(lbmh::launch_heat(s->c, report != 0, (cudaStream_t)stream));
     s->c.g_cur ^= 1;
@@ -624,6 +631,7 @@ lbm_status lbm_run(lbm_solver *s, int32_t count, int32_t report_last, void *stre
   lbmh::Range range_("lbm_run");
   LBM_HANDLE(s);
   if (count < 0) return fail(LBM_ERR_ARG, "count must be >= 0");
+  if (s->c.starve_next) return fail(LBM_ERR_STATE, "a stall test is pending: it applies to lbm_step only");
   const cudaStream_t st = (cudaStream_t)stream;
   const int32_t quiet = report_last ? count - 1 : count;
   int32_t k = 0;
@@ -653,7 +661,10 @@ static lbm_status check_kernel_error(lbm_solver *s) {
   LBM_CUDA(cudaMemcpy(&flag, s->c.error, sizeof(flag), cudaMemcpyDeviceToHost));
   if (flag) {
     cudaMemset(s->c.error, 0, sizeof(flag));
-    return fail(LBM_ERR_CUDA, "a step kernel gave up waiting for its copies; the populations are invalid");
+    return fail(LBM_ERR_CUDA, (flag & lbmk::STREAM_IN_FLIGHT)
+                                  ? "a step kernel gave up waiting for its copies, and some were still "
+                                    "unconfirmed when it ended; the populations are invalid"
+                                  : "a step kernel gave up waiting for its copies; the populations are invalid");
   }
   return LBM_OK;
 }
@@ -966,6 +977,15 @@ lbm_status lbm_timing_read(lbm_solver *s, double out[7]) {
 lbm_status lbm_sync(lbm_solver *s) {
   LBM_HANDLE(s);
   return check_kernel_error(s);
+}
+
+lbm_status lbm_test_bulkcopy_stall(lbm_solver *s, int64_t wait_polls) {
+  LBM_HANDLE(s);
+  if (!s->c.use_stream) return fail(LBM_ERR_STATE, "the solver does not use the bulk-copy kernel");
+  if (wait_polls < 1) return fail(LBM_ERR_ARG, "wait_polls must be >= 1");
+  s->c.starve_next = 1;
+  s->c.wait_limit = wait_polls;
+  return LBM_OK;
 }
 
 lbm_status lbm_heat_field(lbm_solver *s, int32_t id, float **ptr) {

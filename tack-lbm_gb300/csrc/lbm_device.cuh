@@ -379,6 +379,23 @@ __device__ __forceinline__ void eq_pairs(T rv, T rho, T ux, T uy, T uz, T A[9], 
   });
 }
 
+// The equilibrium of one pair formed where it is used (the same arithmetic as
+// eq_pairs), so that no array of A and B stays live across the collision.
+template <typename T>
+struct EqBase {
+  T base, r45, r3;
+};
+template <typename T>
+__device__ __forceinline__ EqBase<T> eq_base(T rv, T rho, T ux, T uy, T uz) {
+  return EqBase<T>{rv - T(1.5) * rho * (ux * ux + uy * uy + uz * uz), T(4.5) * rho, T(3.0) * rho};
+}
+template <typename T, int k>
+__device__ __forceinline__ void eq_pair(const EqBase<T> &e, T ux, T uy, T uz, T &A, T &B) {
+  const T sd = pair_dot<T, k>(ux, uy, uz);
+  A = e.r45 * sd * sd + e.base;
+  B = e.r3 * sd;
+}
+
 // equilibrium values of all 19 directions
 template <typename T, bool DEV>
 __device__ __forceinline__ void feq_val(T rv, T rho, T ux, T uy, T uz, T eq[Q]) {
@@ -398,20 +415,23 @@ __device__ __forceinline__ T rv_of(const Moments<T> &m) {
 }
 
 // v <- v + om (feq - v), written v (1 - om) + om feq: with om w A and om w B
-// formed once per pair that is one fused multiply-add per population.
+// formed once per pair that is one fused multiply-add per population. The
+// pairs' A and B are formed as each pair is relaxed.
 template <typename T>
-__device__ __forceinline__ void relax_bgk(T v[Q], T om, const T A[9], const T B[9], T eq0) {
+__device__ __forceinline__ void relax_bgk(T v[Q], T om, const EqBase<T> &e, T ux, T uy, T uz) {
   const T keep = T(1) - om;
   const T om1 = om * T(wq(1)), om7 = om * T(wq(7));
-  v[0] = v[0] * keep + om * eq0;
-#pragma unroll
-  for (int k = 0; k < 9; ++k) {
-    const int q = pq(k);
+  v[0] = v[0] * keep + om * (T(wq(0)) * e.base);
+  static_for<9>([&](auto kc) {
+    constexpr int k = decltype(kc)::value;
+    constexpr int q = pq(k);
+    T A, B;
+    eq_pair<T, k>(e, ux, uy, uz, A, B);
     const T ow = k < 3 ? om1 : om7;
-    const T oA = ow * A[k], oB = ow * B[k];
+    const T oA = ow * A, oB = ow * B;
     v[q] = v[q] * keep + (oA + oB);
     v[q + 1] = v[q + 1] * keep + (oA - oB);
-  }
+  });
 }
 
 // Relax the values v[] in place: BGK (lbm.py:60-69), TRT + Smagorinsky
@@ -421,10 +441,9 @@ __device__ __forceinline__ void relax_bgk(T v[Q], T om, const T A[9], const T B[
 template <typename T, int COLL, bool DEV>
 __device__ __forceinline__ T collide(T v[Q], const Moments<T> &m, const Pairs<T> &pr, T omega_bgk, T tau0,
                                      T smag_c, T magic) {
-  T A[9], B[9], eq0;
-  eq_pairs<T, DEV>(rv_of<T, DEV>(m), m.rho, m.ux, m.uy, m.uz, A, B, eq0);
+  const EqBase<T> e = eq_base<T>(rv_of<T, DEV>(m), m.rho, m.ux, m.uy, m.uz);
   if (COLL == COLL_BGK) {
-    relax_bgk<T>(v, omega_bgk, A, B, eq0);
+    relax_bgk<T>(v, omega_bgk, e, m.ux, m.uy, m.uz);
     return tau0;
   }
   // Smagorinsky relaxation time from the non-equilibrium stress (lbm.py:72-93)
@@ -442,41 +461,52 @@ __device__ __forceinline__ T collide(T v[Q], const Moments<T> &m, const Pairs<T>
   const T pi = sqrt_fast<T>(pxx * pxx + pyy * pyy + pzz * pzz + T(2) * (pxy * pxy + pxz * pxz + pyz * pyz));
   const T tau = T(0.5) * (tau0 + sqrt_fast<T>(tau0 * tau0 + smag_c * pi * rcp_fast<T>(m.rho)));
   if (COLL == COLL_LES) {
-    relax_bgk<T>(v, rcp_fast<T>(tau), A, B, eq0);
+    relax_bgk<T>(v, rcp_fast<T>(tau), e, m.ux, m.uy, m.uz);
     return tau;
   }
   // TRT: even/odd parts relaxed at omega+ = 1/tau, omega- = 1/(magic/(tau-1/2)+1/2)
   const T hp = T(0.5) * rcp_fast<T>(tau);
   const T hm = T(0.5) * rcp_fast<T>(magic * rcp_fast<T>(tau - T(0.5)) + T(0.5));
-  v[0] += T(2) * hp * (eq0 - v[0]);
-#pragma unroll
-  for (int k = 0; k < 9; ++k) {
-    const int q = pq(k);
+  v[0] += T(2) * hp * (T(wq(0)) * e.base - v[0]);
+  static_for<9>([&](auto kc) {
+    constexpr int k = decltype(kc)::value;
+    constexpr int q = pq(k);
+    T A, B;
+    eq_pair<T, k>(e, m.ux, m.uy, m.uz, A, B);
     const T w2 = T(2) * T(wq(q));
     // D_k - 2 w (A - rv + drho): the symmetric non-equilibrium part in deviations
-    const T sym = hp * (pr.D[k] - w2 * (A[k] - (DEV ? T(0) : T(1))));
-    const T anti = hm * (pr.M[k] - w2 * B[k]);
+    const T sym = hp * (pr.D[k] - w2 * (A - (DEV ? T(0) : T(1))));
+    const T anti = hm * (pr.M[k] - w2 * B);
     v[q] = v[q] - sym - anti;
     v[q + 1] = v[q + 1] - sym + anti;
-  }
+  });
   return tau;
 }
 
 // Sponge blend toward (1, u0*fluid, 0, 0) (lbm.py:446-456):
 // out = feq(rho_s, u_s) + (1 - sigma)(post - feq(rho, u)), in values.
+// The two equilibria are formed pair by pair as they are used.
 template <typename T, bool DEV>
 __device__ __forceinline__ void sponge(T v[Q], const Moments<T> &m, T sigma, T u0fluid) {
-  T e0[Q], e1[Q];
-  feq_val<T, DEV>(rv_of<T, DEV>(m), m.rho, m.ux, m.uy, m.uz, e0);
+  const EqBase<T> e0 = eq_base<T>(rv_of<T, DEV>(m), m.rho, m.ux, m.uy, m.uz);
   const T drho_s = m.drho - sigma * m.drho;
   const T rho_s = T(1) + drho_s;
   const T ux_s = m.ux + sigma * (u0fluid - m.ux);
   const T uy_s = (T(1) - sigma) * m.uy;
   const T uz_s = (T(1) - sigma) * m.uz;
-  feq_val<T, DEV>(DEV ? drho_s : rho_s, rho_s, ux_s, uy_s, uz_s, e1);
+  const EqBase<T> e1 = eq_base<T>(DEV ? drho_s : rho_s, rho_s, ux_s, uy_s, uz_s);
   const T keep = T(1) - sigma;
-#pragma unroll
-  for (int q = 0; q < Q; ++q) v[q] = e1[q] + keep * (v[q] - e0[q]);
+  v[0] = T(wq(0)) * e1.base + keep * (v[0] - T(wq(0)) * e0.base);
+  static_for<9>([&](auto kc) {
+    constexpr int k = decltype(kc)::value;
+    constexpr int q = pq(k);
+    const T w = T(wq(q));
+    T A0, B0, A1, B1;
+    eq_pair<T, k>(e0, m.ux, m.uy, m.uz, A0, B0);
+    eq_pair<T, k>(e1, ux_s, uy_s, uz_s, A1, B1);
+    v[q] = w * (A1 + B1) + keep * (v[q] - w * (A0 + B0));
+    v[q + 1] = w * (A1 - B1) + keep * (v[q + 1] - w * (A0 - B0));
+  });
 }
 
 // ---------------------------------------------------------------------------
@@ -679,6 +709,35 @@ __device__ __forceinline__ Offsets<S> cell_offsets(const StepArgs<S> &a, int x, 
   return o;
 }
 
+// An odd step stores each population where it read one (src_loc), so the 19
+// load addresses could simply be kept for the stores: 19 pointers live across
+// the whole collision. opaque_store<S>() forms the store addresses again from
+// copies of the cell index and offsets the compiler cannot identify with the
+// originals, which keeps 7 integers live instead. That frees the registers
+// for more FP32 blocks per SM (below); the 2-byte storages, which sit at 72
+// registers either way, ran 2 % slower with it, and FP64 does not use it.
+#ifndef LBM_OPAQUE_STORE_16
+#define LBM_OPAQUE_STORE_16 0
+#endif
+#ifndef LBM_OPAQUE_STORE_32
+#define LBM_OPAQUE_STORE_32 1
+#endif
+template <typename S>
+__host__ __device__ constexpr bool opaque_store() {
+  return sizeof(S) == 2 ? LBM_OPAQUE_STORE_16 != 0 : sizeof(S) == 4 && LBM_OPAQUE_STORE_32 != 0;
+}
+
+// a copy of v the compiler cannot see through (no common subexpression with v)
+__device__ __forceinline__ int opaque(int v) {
+  int r;
+  asm volatile("mov.b32 %0, %1;" : "=r"(r) : "r"(v));
+  return r;
+}
+template <typename S>
+__device__ __forceinline__ Offsets<S> opaque(const Offsets<S> &o) {
+  return Offsets<S>{opaque(o.dxm), opaque(o.dxp), opaque(o.dym), opaque(o.dyp), opaque(o.dzm), opaque(o.dzp)};
+}
+
 template <typename S>
 __device__ __forceinline__ Row row_of(const StepArgs<S> &a, int y, int z) {
   Row r;
@@ -737,6 +796,25 @@ __device__ __forceinline__ void fast_load(const StepArgs<S> &a, int idx, const O
   });
 }
 
+// Moments, collision, temperature coupling and sponge of a fluid cell (x, idx)
+// with inputs d[]; d[] becomes the post-collision populations.
+template <typename S, int COLL>
+__device__ __forceinline__ Moments<typename Store<S>::T> fluid_update(const StepArgs<S> &a, int x, int idx,
+                                                                     typename Store<S>::T d[Q]) {
+  using T = typename Store<S>::T;
+  constexpr bool DEV = Store<S>::DEV;
+  Pairs<T> pr;
+  const Moments<T> mo = moments<T, DEV>(d, true, pr);
+  const T tau = collide<T, COLL, DEV>(d, mo, pr, a.omega_bgk, a.tau0, a.smag_c, a.magic);
+  if (a.aux) a.aux[idx] = make_float4((float)mo.ux, (float)mo.uy, (float)mo.uz, (float)tau);
+  const T t = fmax(T(0), (T(x) - a.sponge_start) * a.inv_sponge_len);
+  const T sigma = a.sponge_strength * t * t;
+  if (sigma != T(0)) sponge<T, DEV>(d, mo, sigma, a.u0);
+  return mo;
+}
+
+// The rest of the cell's step after fast_load: bounce-back links, the update,
+// the stores and the report fields.
 template <typename S, int COLL, bool REPORT, bool ODD, bool SPECIAL>
 __device__ __forceinline__ void fast_finish(const StepArgs<S> &a, int x, int y, int idx, const Offsets<S> &o,
                                             const Row &r, uint32_t m, typename Store<S>::T d[Q], const Prev &prev,
@@ -765,20 +843,20 @@ __device__ __forceinline__ void fast_finish(const StepArgs<S> &a, int x, int y, 
       }
     });
   }
-  Pairs<T> pr;
-  const Moments<T> mo = moments<T, DEV>(d, !here, pr);
+  Moments<T> mo;
   if (!here) {
-    const T tau = collide<T, COLL, DEV>(d, mo, pr, a.omega_bgk, a.tau0, a.smag_c, a.magic);
-    if (a.aux) a.aux[idx] = make_float4((float)mo.ux, (float)mo.uy, (float)mo.uz, (float)tau);
-    const T t = fmax(T(0), (T(x) - a.sponge_start) * a.inv_sponge_len);
-    const T sigma = a.sponge_strength * t * t;
-    if (sigma != T(0)) sponge<T, DEV>(d, mo, sigma, a.u0);
+    mo = fluid_update<S, COLL>(a, x, idx, d);
+    const int idx_s = opaque_store<S>() ? opaque(idx) : idx;
+    const Offsets<S> o_s = opaque_store<S>() ? opaque(o) : o;
     static_for<Q>([&](auto pc) {
       constexpr int p = decltype(pc)::value;
       // population p moves to x + c_p: the odd-step source location of direction opp(p)
-      if (ODD) Store<S>::template gstore<p>(src_loc<opp(p), SPECIAL>(a, idx, o, r), d[p]);
+      if (ODD) Store<S>::template gstore<p>(src_loc<opp(p), SPECIAL>(a, idx_s, o_s, r), d[p]);
       else Store<S>::template gstore<p>(a.slot[opp(p)] + idx, d[p]);
     });
+  } else {
+    Pairs<T> pr;
+    mo = moments<T, DEV>(d, false, pr);
   }
   if (REPORT) diagnostics<T>(a.fld, idx, mo, mx, my, mz, prev, v);
 }
@@ -924,19 +1002,26 @@ __device__ __forceinline__ bool lid_row(const StepArgs<S> &a, int y) {
   return a.lateral == SIDE_LID && y == a.ny - 1;
 }
 
-// Resident step_kernel blocks per SM, by storage width. FP32 stays at 5
-// blocks (20 warps, no spills; 24 warps measured no faster). FP16/BF16 are
-// latency-bound with half the bytes in flight per warp: 7 blocks (28 warps,
-// 72 registers) run 9 % faster despite spills to L1 (6: 3 %, 8: 7 %, 10: 3 %).
+// Resident step_kernel blocks per SM, by storage width. FP32 runs 8 blocks
+// (32 warps, 64 registers) with the odd step's store addresses formed again
+// (opaque_store): 0.203 ms per C2 launch, against 0.206 at 7 blocks,
+// 0.223-0.230 at 6 and 0.225 at 5 (the earlier 5 blocks without
+// opaque_store). FP16/BF16 are latency-bound with half the bytes in flight
+// per warp: 7 blocks (28 warps, 72 registers) ran 9 % faster than 5 despite
+// spills to L1 (6: 3 %, 8: 7-11 %, 10: 3 %). FP64 (the oracle-precision
+// runs, twice the registers per value) keeps 5.
 #ifndef LBM_STEP_MIN_BLOCKS
-#define LBM_STEP_MIN_BLOCKS 5
+#define LBM_STEP_MIN_BLOCKS 8
 #endif
 #ifndef LBM_STEP_MIN_BLOCKS_16
 #define LBM_STEP_MIN_BLOCKS_16 7
 #endif
+#ifndef LBM_STEP_MIN_BLOCKS_64
+#define LBM_STEP_MIN_BLOCKS_64 5
+#endif
 template <typename S>
 __host__ __device__ constexpr int step_min_blocks() {
-  return sizeof(S) == 2 ? LBM_STEP_MIN_BLOCKS_16 : LBM_STEP_MIN_BLOCKS;
+  return sizeof(S) == 2 ? LBM_STEP_MIN_BLOCKS_16 : sizeof(S) == 8 ? LBM_STEP_MIN_BLOCKS_64 : LBM_STEP_MIN_BLOCKS;
 }
 
 // One cell of the per-cell kernels: the warp is the 32-cell row segment at x0.

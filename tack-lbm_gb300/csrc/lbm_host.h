@@ -80,6 +80,8 @@ struct Ctx {
   int64_t bulk_cells, generic_cells;
   // bulk-copy (TMA) path: row segments of lbmk::SW cells
   int use_stream;            // 1 when nx suits 16-byte row pieces
+  long long wait_limit;      // bulk-copy kernel: mbarrier polls before a wait gives up
+  int starve_next;           // test hook: the next bulk-copy step issues no copies (lbm_test_bulkcopy_stall)
   int nseg_x, nseg;          // segments per row, segments in the lattice
   int *seg_mask;             // per segment: first link-mask word or -1
   int *seg_list;             // the masked segments

@@ -81,6 +81,8 @@ cudaError_t launch_variant(const Ctx &c, const StepArgs<S> &a, cudaStream_t st, 
     sa.seg_mask = c.seg_mask;
     sa.masks = c.masks;
     sa.error = c.error;
+    sa.wait_limit = c.wait_limit;
+    sa.starve = c.starve_next;
     const int grid = stream_grid<S, COLL, REPORT, ODD>(c);
     stream_kernel<S, COLL, REPORT, ODD><<<grid, SW + 32, Layout<S>::BYTES, st>>>(sa);
     *rows = grid;

@@ -31,7 +31,11 @@
 namespace lbmk {
 
 constexpr int SW = 256;  // cells per segment = threads per CTA
-constexpr long long WAIT_LIMIT = 1ll << 20;  // mbarrier polls before a step gives up
+constexpr long long WAIT_LIMIT = 1ll << 20;  // default mbarrier polls before a step gives up
+
+// Bits of StreamArgs::error.
+constexpr unsigned int STREAM_GAVE_UP = 1u;     // a wait ran out: the step's populations are invalid
+constexpr unsigned int STREAM_IN_FLIGHT = 2u;   // a CTA ended with copies into its shared memory unconfirmed
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -75,7 +79,9 @@ struct StreamArgs {
   int nseg;                 // segments in the lattice
   const int *seg_mask;      // per segment: first mask word, or -1 (no obstacle within reach)
   const uint32_t *masks;    // link masks, SW words per masked segment
-  unsigned int *error;      // nonzero after a wait gave up
+  unsigned int *error;      // STREAM_* bits after a wait gave up
+  long long wait_limit;     // mbarrier polls before a wait gives up
+  int starve;               // test hook: the producer issues no copies, so every consumer wait runs out
 };
 
 // One segment: row (y, z), cells [x0, x0 + w), first link-mask word (or -1).
@@ -177,6 +183,7 @@ __device__ __forceinline__ void issue_loads(const StreamArgs<S> &sa, const DirTa
   const StepArgs<S> &a = sa.a;
   const SegInfo g = decode_seg(sa, seg);
   if (lane == 0) *info = g;
+  if (sa.starve) return;  // no arrival and no copy: the stage's `full` phase never completes
   Piece p{0, 0, 0, 0};
   uint32_t bytes = 0;
   if (lane < Q) {
@@ -327,10 +334,10 @@ __device__ __forceinline__ void stream_cell(const StepArgs<S> &a, const SegInfo 
   if (REPORT) diagnostics<T>(a.fld, idx, mo, mx, my, mz, prev, v);
 }
 
-__device__ __forceinline__ bool wait_phase(uint64_t *bar, uint32_t parity) {
+__device__ __forceinline__ bool wait_phase(uint64_t *bar, uint32_t parity, long long limit) {
   long long polls = 0;
   while (!mbar_try_wait(bar, parity))
-    if (++polls > WAIT_LIMIT) return false;
+    if (++polls > limit) return false;
   return true;
 }
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
@@ -354,6 +361,7 @@ __global__ void __launch_bounds__(SW + 32) stream_kernel(const __grid_constant__
   __shared__ CSum red[SW / 32][NSUM];
   __shared__ DirTab tab[Q];
   __shared__ SegInfo info[L::NST];
+  __shared__ volatile int gave_up;  // a consumer's wait ran out: the producer issues nothing more
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
   // this CTA's segments: blockIdx.x, blockIdx.x + gridDim.x, ...
@@ -361,6 +369,7 @@ __global__ void __launch_bounds__(SW + 32) stream_kernel(const __grid_constant__
   const int count = first < sa.nseg ? (sa.nseg - 1 - first) / stride + 1 : 0;
   fill_dirtab(tab, tid);
   if (tid == 0) {
+    gave_up = 0;
     for (int s = 0; s < NST; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], SW / 32);
@@ -373,14 +382,20 @@ __global__ void __launch_bounds__(SW + 32) stream_kernel(const __grid_constant__
   if (warp == SW / 32) {
     // producer warp: NST-1 segments ahead; a stage is refilled one iteration
     // after its stores were issued, so they have drained by then
-    for (int k = 0; k < NST - 1 && k < count; ++k)
+    int issued = 0;  // segments [0, issued) have had their loads issued
+    for (int k = 0; k < NST - 1 && k < count; ++k) {
       issue_loads<S, ODD>(sa, tab, first + k * stride, stages + k * L::STAGE, &full[k], &info[k], lane);
-    for (int it = 0; it < count; ++it) {
+      issued = sa.starve ? 0 : k + 1;
+    }
+    int it = 0;
+    for (; it < count; ++it) {
       const int st = it % NST;
-      if (!__all_sync(0xffffffffu, wait_phase(&empty[st], (uint32_t)((it / NST) & 1)))) {
-        if (lane == 0) atomicOr(sa.error, 1u);
+      if (!__all_sync(0xffffffffu, wait_phase(&empty[st], (uint32_t)((it / NST) & 1), sa.wait_limit))) {
+        if (lane == 0) atomicOr(sa.error, STREAM_GAVE_UP);
         break;
       }
+      // the consumers' arrival for segment it carries their gave_up store
+      if (gave_up) break;
       issue_stores<S, ODD>(sa, tab, info[st], stages + st * L::STAGE, lane);
       const int nxt = it + NST - 1;
       if (nxt < count) {
@@ -388,8 +403,17 @@ __global__ void __launch_bounds__(SW + 32) stream_kernel(const __grid_constant__
         bulk_wait_read_1();        // this lane's stores of segment it-1 have read their buffer
         __syncwarp();
         issue_loads<S, ODD>(sa, tab, first + nxt * stride, stages + ns * L::STAGE, &full[ns], &info[ns], lane);
+        if (!sa.starve) issued = nxt + 1;
       }
     }
+    // Given up: segments it .. issued-1 may still have loads landing in this
+    // CTA's shared memory (each in its own stage, one phase each, since no
+    // stage was refilled before its consumers were done). Wait for them,
+    // within the limit, before the CTA ends; the stages of segments before
+    // `it` were all confirmed by the consumers.
+    for (int j = it; j < issued; ++j)
+      if (!wait_phase(&full[j % NST], (uint32_t)((j / NST) & 1), sa.wait_limit) && lane == 0)
+        atomicOr(sa.error, STREAM_IN_FLIGHT);
     bulk_wait_all();
     return;
   }
@@ -402,13 +426,16 @@ __global__ void __launch_bounds__(SW + 32) stream_kernel(const __grid_constant__
   for (int it = 0; it < count; ++it) {
     const int st = it % NST;
     S *stage = stages + st * L::STAGE;
-    // After a wait gave up, the error is flagged and the remaining segments are
-    // passed through without waiting: every barrier is still met, nothing hangs.
-    if (!bad && !wait_phase(&full[st], (uint32_t)((it / NST) & 1))) {
-      atomicOr(sa.error, 1u);
+    // After a wait gave up, the error is flagged, the producer is told to
+    // issue nothing more, and this thread passes the remaining segments
+    // through without waiting or touching memory: every barrier is still met,
+    // nothing hangs.
+    if (!bad && !wait_phase(&full[st], (uint32_t)((it / NST) & 1), sa.wait_limit)) {
+      atomicOr(sa.error, STREAM_GAVE_UP);
+      gave_up = 1;
       bad = true;
     }
-    const SegInfo g = info[st];
+    const SegInfo g = bad ? SegInfo{0, 0, 0, 0, -1} : info[st];
     const bool lid_row = sa.a.lateral == SIDE_LID && g.y == sa.a.ny - 1;
     float v[NSUM] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (tid < g.w) {
@@ -428,7 +455,7 @@ __global__ void __launch_bounds__(SW + 32) stream_kernel(const __grid_constant__
     }
     if (ODD) {
       consumer_sync();  // the edge elements were written by other threads
-      edge_stores<S, ODD>(sa, tab, g, stage, tid);
+      if (!bad) edge_stores<S, ODD>(sa, tab, g, stage, tid);
     }
     fence_async_smem();  // this thread's shared-memory writes, before the bulk stores read them
     __syncwarp();

@@ -124,6 +124,7 @@ _SIGNATURES = {
     "lbm_step_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
     "lbm_memory": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
     "lbm_sync": (ctypes.c_int, [ctypes.c_void_p]),
+    "lbm_test_bulkcopy_stall": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64]),
     "lbm_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "lbm_timing_read": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
     "lbm_field_sums_static": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int64,

@@ -196,7 +196,27 @@ def study_c5(steps=5000, every=100, device=0):
     return out
 
 
-def _collision_run(collision, re, steps, every, device):
+def raw_strouhal(lift, every, diameter, u0):
+    """collision_check.py's estimator (collision_check.py:27-30): the raw rFFT
+    peak of the mean-removed second half of a lift history sampled every
+    ``every`` steps, as St = f D / U; returns (St, the grid's bin width)."""
+    cl = np.asarray(lift[len(lift) // 2:], np.float64)
+    cl = cl - cl.mean()
+    spec = np.abs(np.fft.rfft(cl))
+    freq = np.fft.rfftfreq(len(cl), d=every)
+    k = int(np.argmax(spec[1:]) + 1)
+    scale = diameter / u0
+    return float(freq[k] * scale), float(freq[1] * scale)
+
+
+# run lengths (steps) at which collision_check.py's raw estimator is evaluated
+# on the long Re 300 histories: their second halves put St on grids of
+# 0.1, 0.075, 0.05, 0.0375, 0.03, 0.025 and 0.02 (0.200 is on all but 0.075,
+# 0.0375 and 0.03)
+RAW_LENGTHS = (6000, 8000, 12000, 16000, 20000, 24000, 30000)
+
+
+def _collision_run(collision, re, steps, every, device, raw_lengths=()):
     """One collision_check.py run (collision_check.py:12-31): the default Solver
     (384x128x64, cylinder D = 24, U = 0.08, periodic y and z, lbm_init start) at
     Reynolds number ``re``, ``every - 1`` quiet steps and one report step per
@@ -222,12 +242,15 @@ def _collision_run(collision, re, steps, every, device):
         return r
     cl = np.array(lift[len(lift) // 2:])
     cl -= cl.mean()
-    spec = np.abs(np.fft.rfft(cl))
-    freq = np.fft.rfftfreq(len(cl), d=every)
-    k = int(np.argmax(spec[1:]) + 1)
-    scale = s.diameter / s.u0
-    r.update(stable=True, cl_amplitude=float(np.abs(cl).max()), strouhal_raw=float(freq[k] * scale),
-             strouhal_bin=float(freq[1] * scale), strouhal_refined=strouhal(cl, every, s.diameter, s.u0))
+    st_raw, st_bin = raw_strouhal(lift, every, s.diameter, s.u0)
+    r.update(stable=True, cl_amplitude=float(np.abs(cl).max()), strouhal_raw=st_raw,
+             strouhal_bin=st_bin, strouhal_refined=strouhal(cl, every, s.diameter, s.u0))
+    if raw_lengths:
+        # what collision_check.py prints when run for n steps: the same
+        # deterministic history cut at n
+        r["raw_by_steps"] = {str(n): dict(zip(("strouhal_raw", "strouhal_bin"),
+                                              raw_strouhal(lift[:n // every], every, s.diameter, s.u0)))
+                             for n in raw_lengths if n <= steps}
     return r
 
 
@@ -244,7 +267,8 @@ def study_collision(steps=8000, every=50, long_steps=30000, device=0):
         for coll in ("bgk", "trt", "les"):
             out["runs"].append(_collision_run(coll, re, steps, every, device))
     if long_steps:
-        out["long"] = [_collision_run(coll, 300, long_steps, every, device) for coll in ("bgk", "trt", "les")]
+        out["long"] = [_collision_run(coll, 300, long_steps, every, device, RAW_LENGTHS)
+                       for coll in ("bgk", "trt", "les")]
     runs = {(r["reynolds"], r["collision"]): r for r in out["runs"]}
     out["checks"] = {
         "bgk_diverges_at_re3000": not runs[(3000, "bgk")]["stable"],

@@ -375,6 +375,75 @@ def test_long_rows(G, storage, tol, kernel):
             assert O.weight_err(get(h, cfg.n), f) <= tol, f"{storage} step {k + 1}"
 
 
+def test_bulkcopy_wait_gives_up_and_recovers(G):
+    """The bulk-copy kernel's bounded waits: with lbm_test_bulkcopy_stall the
+    next step's producer issues no copies, so every consumer wait runs out (a
+    wait that nothing can end, not a fault). The step ends by itself, the
+    next lbm_sync reports LBM_ERR_CUDA and clears the state, and a step from
+    re-imported populations matches the oracle again."""
+    lib = N.load()
+    cfg = O.Config(64, 20, 12, collision="les", nu=0.01, obstacle="cylinder", ox=20.3, oy=9.6, r=3.4,
+                   u0=0.07, sponge_start=50.0, sponge_strength=0.9, vertical="slip", omega_rot=0.02)
+    h = native_handle(cfg, flags=N.FLAG_BULKCOPY)
+    h.call("lbm_init_random", 1e-3, 0.01, 9)
+    f0 = get(h, cfg.n)
+    h.call("lbm_test_bulkcopy_stall", 2000)
+    assert h.call("lbm_run", 2, 0, None, allow=(N.ERR_STATE,)) == N.ERR_STATE
+    h.call("lbm_step", 0, None)
+    assert h.call("lbm_sync", allow=(N.ERR_CUDA,)) == N.ERR_CUDA
+    assert b"gave up waiting" in lib.lbm_last_error()
+    assert h.call("lbm_sync") == N.OK
+    put(h, f0)
+    h.call("lbm_step", 0, None)
+    assert h.call("lbm_sync") == N.OK
+    assert O.weight_err(get(h, cfg.n), O.step(cfg, f0).reshape(-1)) <= TOL32
+    # a solver without the bulk-copy kernel has no such hook
+    h2 = native_handle(cfg)
+    assert h2.call("lbm_test_bulkcopy_stall", 10, allow=(N.ERR_STATE,)) == N.ERR_STATE
+
+
+TWO_BYTE_CASES = {
+    "cylinder_slip": dict(obstacle="cylinder", ox=64.3, oy=5.6, r=3.2, omega_rot=0.04, lateral="slip",
+                          vertical="slip"),
+    "box_lid": dict(obstacle="box", ox=127.5, oy=6.0, oz=3.0, hx=3.0, hy=2.5, hz=2.0, lateral="lid",
+                    vertical="periodic", u_lid=0.05),
+    "open_periodic": dict(obstacle="none"),
+}
+
+
+@pytest.mark.parametrize("storage,tol", [("f16", 4e-4), ("bf16", 4e-3)])
+@pytest.mark.parametrize("collision", ["les", "trt", "bgk"])
+@pytest.mark.parametrize("case", list(TWO_BYTE_CASES))
+def test_two_byte_storage_steps_and_fields(G, case, collision, storage, tol):
+    """FP16/BF16 deviation storage with every collision model: rows of six
+    32-cell warps (nx = 192) with wrap-around at both ends, an obstacle across
+    a warp boundary (masked warps beside unmasked ones), slip and lid walls.
+    Five steps (odd, even, odd with a report, even with a report, odd), each
+    against the oracle fed the stored state; the report fields to 1e-6."""
+    cfg = O.Config(192, 12, 6, collision=collision, nu=0.02, u0=0.07, sponge_start=168.0,
+                   sponge_strength=0.9, **TWO_BYTE_CASES[case])
+    h = native_handle(cfg, storage)
+    assert np.array_equal(gpu_mask(h, cfg.n), O.mask(cfg).astype(np.uint8))
+    h.call("lbm_init_random", 1e-3, 0.01, 5)
+    f = get(h, cfg.n)
+    fields = O.new_fields(cfg.n)
+    for k in range(5):
+        rep = k in (2, 3)
+        if rep:
+            # the report's previous fields: the oracle's, in float32 as the GPU keeps them
+            set_fields(h, fields)
+        h.call("lbm_step", int(rep), None)
+        f = O.step(cfg, f, fields, report=rep).reshape(-1)
+        g = get(h, cfg.n)
+        assert O.weight_err(g, f) <= tol, f"{storage} {case} {collision} step {k + 1}"
+        if rep:
+            got = get_fields(h, cfg.n)
+            for name in ("ux", "uy", "uz", "p", "vmag", "fx", "fy", "fz"):
+                err = np.abs(got[name] - fields[name]).max()
+                assert err <= 1e-6, f"{storage} {case} {collision} step {k + 1} {name}: {err:.3e}"
+        f = g
+
+
 @pytest.mark.parametrize("kind", ["les_slipz", "lid_box", "heatsink_heat", "bulkcopy", "f16"])
 def test_run_graphs_match_single_steps(G, kind):
     """lbm_run launches pairs of quiet steps as CUDA graphs: the result is the
