@@ -75,11 +75,14 @@ constexpr int NPAR = 4;  // U, tau0, Cs, r
 
 // Resident blocks per SM of the forward and reverse kernels in float32 (the
 // timed precision); float64 leaves the register count to the compiler.
+// Measured on the 256x128x32 adjoint (forward / backward ms): the compiler's
+// own choice (96 and 168 registers, 5 and 3 blocks) 77.6 / 222.5; 6 and 4
+// blocks 72.8 / 211.7; 8 and 4 blocks (64 and 128 registers) 66.7 / 206.2.
 #ifndef LBM_ADJ_STEP_MIN_BLOCKS
-#define LBM_ADJ_STEP_MIN_BLOCKS 5
+#define LBM_ADJ_STEP_MIN_BLOCKS 8
 #endif
 #ifndef LBM_ADJ_REVERSE_MIN_BLOCKS
-#define LBM_ADJ_REVERSE_MIN_BLOCKS 3
+#define LBM_ADJ_REVERSE_MIN_BLOCKS 4
 #endif
 template <typename T>
 constexpr int adj_step_blocks() {
@@ -244,7 +247,7 @@ __device__ __forceinline__ void forward_cell(const DArgs<T> &a, int x, T fl, con
   F.fl = fl;
   F.drho = sum + T(W_EXCESS);
   F.rho = T(1) + F.drho;
-  F.inv = T(1) / F.rho;
+  F.inv = rcp_fast<T>(F.rho);
   F.jx = M[0] + M[3] + M[4] + M[5] + M[6];
   F.jy = M[1] + M[3] - M[4] + M[7] + M[8];
   F.jz = M[2] + M[5] - M[6] + M[7] - M[8];
@@ -266,11 +269,11 @@ __device__ __forceinline__ void forward_cell(const DArgs<T> &a, int x, T fl, con
   F.pi[3] = (D[3] - D[4]) - offd * F.ux * F.uy;
   F.pi[4] = (D[5] - D[6]) - offd * F.ux * F.uz;
   F.pi[5] = (D[7] - D[8]) - offd * F.uy * F.uz;
-  F.pn = sqrt(F.pi[0] * F.pi[0] + F.pi[1] * F.pi[1] + F.pi[2] * F.pi[2] +
-              T(2) * (F.pi[3] * F.pi[3] + F.pi[4] * F.pi[4] + F.pi[5] * F.pi[5]));
+  F.pn = sqrt_fast<T>(F.pi[0] * F.pi[0] + F.pi[1] * F.pi[1] + F.pi[2] * F.pi[2] +
+                     T(2) * (F.pi[3] * F.pi[3] + F.pi[4] * F.pi[4] + F.pi[5] * F.pi[5]));
   F.c = T(SMAG) * a.cs * a.cs;
-  F.root = sqrt(a.tau0 * a.tau0 + F.c * F.pn * F.inv);
-  F.om = T(1) / (T(0.5) * (a.tau0 + F.root));
+  F.root = sqrt_fast<T>(a.tau0 * a.tau0 + F.c * F.pn * F.inv);
+  F.om = rcp_fast<T>(T(0.5) * (a.tau0 + F.root));
   const T t = fmax(T(0), (T(x) - a.sponge_start) * a.inv_sponge_len);
   F.sp = a.sponge_strength * t * t;
   F.sigma = T(1) - fl * (T(1) - F.sp);
@@ -324,12 +327,27 @@ __device__ __forceinline__ T step_cell(const DArgs<T> &a, int x, int idx, const 
   const T fl = BAND ? T(1) - __ldg(a.phi + idx) : T(1);
   Fwd<T> F;
   forward_cell(a, x, fl, g, F);
-  // out = feq(rho_s, u_s) + keep (post - feq) = feq_s + keep (1 - om) (g - feq)
+  // out = feq(rho_s, u_s) + keep (post - feq) = feq_s + keep (1 - om) (g - feq),
+  // the equilibria in the pair form w (A +- B) (lbm_device.cuh, eq_pair);
+  // with sigma = 0 (fluid outside the sponge) feq_s is feq itself
   const T alpha = F.keep * (T(1) - F.om);
-  static_for<Q>([&](auto qc) {
-    constexpr int q = decltype(qc)::value;
-    const T ne = g[q] - dfeq<T, q>(F.drho, F.rho, F.ux, F.uy, F.uz, F.usq);
-    a.fout[q * a.n + idx] = dfeq<T, q>(F.drhos, F.rhos, F.usx, F.usy, F.usz, F.usqs) + alpha * ne;
+  const EqBase<T> e = eq_base<T>(F.drho, F.rho, F.ux, F.uy, F.uz);
+  const EqBase<T> es = F.sigma == T(0) ? e : eq_base<T>(F.drhos, F.rhos, F.usx, F.usy, F.usz);
+  const T usx = F.sigma == T(0) ? F.ux : F.usx, usy = F.sigma == T(0) ? F.uy : F.usy,
+          usz = F.sigma == T(0) ? F.uz : F.usz;
+  {
+    const T f0 = T(wq(0)) * e.base;
+    a.fout[idx] = T(wq(0)) * es.base + alpha * (g[0] - f0);
+  }
+  static_for<9>([&](auto kc) {
+    constexpr int k = decltype(kc)::value;
+    constexpr int q = pq(k);
+    const T w = T(wq(q));
+    T A, B, As, Bs;
+    eq_pair<T, k>(e, F.ux, F.uy, F.uz, A, B);
+    eq_pair<T, k>(es, usx, usy, usz, As, Bs);
+    a.fout[q * a.n + idx] = w * (As + Bs) + alpha * (g[q] - w * (A + B));
+    a.fout[(q + 1) * a.n + idx] = w * (As - Bs) + alpha * (g[q + 1] - w * (A - B));
   });
   return BAND && a.beta != T(0) ? cell_force(a, idx, o, fl) : T(0);
 }
@@ -360,11 +378,19 @@ __device__ __forceinline__ void adjoint_cell(const DArgs<T> &a, int x, int idx, 
   const T phx = BAND ? __ldg(a.phi + idx) : T(0);
   Fwd<T> F;
   forward_cell(a, x, T(1) - phx, g, F);
-  // g <- ne = g - feq(rho, u)
-  static_for<Q>([&](auto qc) {
-    constexpr int q = decltype(qc)::value;
-    g[q] -= dfeq<T, q>(F.drho, F.rho, F.ux, F.uy, F.uz, F.usq);
-  });
+  // g <- ne = g - feq(rho, u), feq in the pair form of step_cell
+  {
+    const EqBase<T> e = eq_base<T>(F.drho, F.rho, F.ux, F.uy, F.uz);
+    g[0] -= T(wq(0)) * e.base;
+    static_for<9>([&](auto kc) {
+      constexpr int k = decltype(kc)::value;
+      constexpr int q = pq(k);
+      T A, B;
+      eq_pair<T, k>(e, F.ux, F.uy, F.uz, A, B);
+      g[q] -= T(wq(q)) * (A + B);
+      g[q + 1] -= T(wq(q)) * (A - B);
+    });
+  }
   // adjoint of the outputs f_t[q](x)
   T ob[Q];
   static_for<Q>([&](auto qc) {
@@ -392,14 +418,14 @@ __device__ __forceinline__ void adjoint_cell(const DArgs<T> &a, int x, int idx, 
   T flb = usbx * F.sigma * a.u0 - sigb * (T(1) - F.sp);
   // om = 1/tau, tau = (tau0 + root)/2, root^2 = tau0^2 + c pn / rho
   const T taub = -omb * F.om * F.om;
-  const T innerb = taub / (T(4) * F.root);
+  const T innerb = taub * rcp_fast<T>(T(4) * F.root);
   grad[1] += T(0.5) * taub + innerb * T(2) * a.tau0;
   grad[2] += innerb * F.pn * F.inv * T(SMAG) * T(2) * a.cs;
   const T pnb = innerb * F.c * F.inv;
   rhob -= innerb * F.c * F.pn * F.inv * F.inv;
   T pib[6] = {0, 0, 0, 0, 0, 0};
   if (F.pn > T(0)) {
-    const T s = pnb / F.pn;
+    const T s = pnb * rcp_fast<T>(F.pn);
     pib[0] = s * F.pi[0];
     pib[1] = s * F.pi[1];
     pib[2] = s * F.pi[2];

@@ -103,6 +103,9 @@ template <typename S>
 struct StepArgs {
   using P = typename Store<S>::T;  // arithmetic precision of the step
   S *slot[Q];             // slot[q] = F + q*n
+  S *F;                   // slot 0
+  uint32_t n;             // cells (the slot stride)
+  int flat;               // 19 n < 2^32: the step kernels address slots by 32-bit offsets from F
   int nx, ny, nz, nxy;
   Geo geo;
   int lateral, vertical;
@@ -748,21 +751,33 @@ __device__ __forceinline__ Row row_of(const StepArgs<S> &a, int y, int z) {
   return r;
 }
 
+// Element e of slot q. FLAT (lattices with 19 n < 2^32, which the step
+// kernels check once per launch) forms it from the one base pointer F and a
+// 32-bit element offset q n + e: two instructions, where the 19 slot
+// pointers of the other form each have to be fetched from the kernel's
+// parameter bank again (registers do not hold them all). 3-7 % faster per
+// C2 launch in FP32 and FP16.
+template <bool FLAT, typename S>
+__device__ __forceinline__ S *slot_at(const StepArgs<S> &a, int q, int e) {
+  if (FLAT) return a.F + (size_t)((uint32_t)q * a.n + (uint32_t)e);
+  return a.slot[q] + e;
+}
+
 // L(x, q): where population q of the cell streams from (odd steps read it there)
-template <int q, bool SPECIAL, typename S>
+template <int q, bool SPECIAL, bool FLAT, typename S>
 __device__ __forceinline__ S *src_loc(const StepArgs<S> &a, int idx, const Offsets<S> &o, const Row &r) {
   const int xp = cx(q) == 1 ? o.dxm : cx(q) == -1 ? o.dxp : 0;
   const int yp = cy(q) == 1 ? o.dym : cy(q) == -1 ? o.dyp : 0;
   const int zp = cz(q) == 1 ? o.dzm : cz(q) == -1 ? o.dzp : 0;
-  if (!SPECIAL) return a.slot[opp(q)] + (idx + xp + yp + zp);
+  if (!SPECIAL) return slot_at<FLAT>(a, opp(q), idx + xp + yp + zp);
   const bool ry = (cy(q) == 1 && r.ylo) || (cy(q) == -1 && r.yhi);
   const bool rz = (cz(q) == 1 && r.zlo) || (cz(q) == -1 && r.zhi);
   constexpr int s00 = opp(q);
   constexpr int s01 = opp(dir(cx(q), cy(q), -cz(q)));
   constexpr int s10 = opp(dir(cx(q), -cy(q), cz(q)));
   constexpr int s11 = opp(dir(cx(q), -cy(q), -cz(q)));
-  S *base = ry ? (rz ? a.slot[s11] : a.slot[s10]) : (rz ? a.slot[s01] : a.slot[s00]);
-  return base + (idx + xp + (ry ? 0 : yp) + (rz ? 0 : zp));
+  const int slot = ry ? (rz ? s11 : s10) : (rz ? s01 : s00);
+  return slot_at<FLAT>(a, slot, idx + xp + (ry ? 0 : yp) + (rz ? 0 : zp));
 }
 
 // moving-wall term 6 w_q c_q.u_w of a bounce link at its midpoint (lbm.py:417-428)
@@ -777,19 +792,19 @@ __device__ __forceinline__ typename Store<S>::T wall_term(const StepArgs<S> &a, 
   return T(6) * T(wq(q)) * (T(cx(q)) * vx + T(cy(q)) * vy);
 }
 
-template <typename S, bool ODD, bool SPECIAL>
+template <typename S, bool ODD, bool SPECIAL, bool FLAT>
 __device__ __forceinline__ void fast_load(const StepArgs<S> &a, int idx, const Offsets<S> &o, const Row &r,
                                           uint32_t m, typename Store<S>::T d[Q]) {
   // (report steps load the previous fields beside this, see load_prev)
   static_for<Q>([&](auto qc) {
     constexpr int q = decltype(qc)::value;
-    S *own = a.slot[q] + idx;
+    S *own = slot_at<FLAT>(a, q, idx);
     const S *addr;
     if (!SPECIAL) {
-      addr = ODD ? src_loc<q, false>(a, idx, o, r) : own;
+      addr = ODD ? src_loc<q, false, FLAT>(a, idx, o, r) : own;
     } else {
       const bool b = (m >> q) & 1u;
-      S *src = src_loc<q, true>(a, idx, o, r);
+      S *src = src_loc<q, true, FLAT>(a, idx, o, r);
       addr = ODD ? (b ? own : src) : (b ? src : own);
     }
     d[q] = Store<S>::template gload<q>(addr);
@@ -815,7 +830,7 @@ __device__ __forceinline__ Moments<typename Store<S>::T> fluid_update(const Step
 
 // The rest of the cell's step after fast_load: bounce-back links, the update,
 // the stores and the report fields.
-template <typename S, int COLL, bool REPORT, bool ODD, bool SPECIAL>
+template <typename S, int COLL, bool REPORT, bool ODD, bool SPECIAL, bool FLAT>
 __device__ __forceinline__ void fast_finish(const StepArgs<S> &a, int x, int y, int idx, const Offsets<S> &o,
                                             const Row &r, uint32_t m, typename Store<S>::T d[Q], const Prev &prev,
                                             float v[NSUM]) {
@@ -851,8 +866,8 @@ __device__ __forceinline__ void fast_finish(const StepArgs<S> &a, int x, int y, 
     static_for<Q>([&](auto pc) {
       constexpr int p = decltype(pc)::value;
       // population p moves to x + c_p: the odd-step source location of direction opp(p)
-      if (ODD) Store<S>::template gstore<p>(src_loc<opp(p), SPECIAL>(a, idx_s, o_s, r), d[p]);
-      else Store<S>::template gstore<p>(a.slot[opp(p)] + idx, d[p]);
+      if (ODD) Store<S>::template gstore<p>(src_loc<opp(p), SPECIAL, FLAT>(a, idx_s, o_s, r), d[p]);
+      else Store<S>::template gstore<p>(slot_at<FLAT>(a, opp(p), idx), d[p]);
     });
   } else {
     Pairs<T> pr;
@@ -1025,7 +1040,7 @@ __host__ __device__ constexpr int step_min_blocks() {
 }
 
 // One cell of the per-cell kernels: the warp is the 32-cell row segment at x0.
-template <typename S, int COLL, bool REPORT, bool ODD>
+template <typename S, int COLL, bool REPORT, bool ODD, bool FLAT>
 __device__ __forceinline__ void cell_step(const StepArgs<S> &a, int x0, int x, int y, int z) {
   using T = typename Store<S>::T;
   float v[NSUM] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -1043,13 +1058,13 @@ __device__ __forceinline__ void cell_step(const StepArgs<S> &a, int x0, int x, i
     Prev prev{0.f, 0.f, 0.f, 0.f};
     if (!(r.ylo || r.yhi || r.zlo || r.zhi) && !walls) {
       if (REPORT) prev = load_prev(a.fld, idx);
-      fast_load<S, ODD, false>(a, idx, o, r, 0u, d);
-      fast_finish<S, COLL, REPORT, ODD, false>(a, x, y, idx, o, r, 0u, d, prev, v);
+      fast_load<S, ODD, false, FLAT>(a, idx, o, r, 0u, d);
+      fast_finish<S, COLL, REPORT, ODD, false, FLAT>(a, x, y, idx, o, r, 0u, d, prev, v);
     } else {
       if (REPORT || !(m & MASK_SOLID)) {
         if (REPORT) prev = load_prev(a.fld, idx);
-        fast_load<S, ODD, true>(a, idx, o, r, m, d);
-        fast_finish<S, COLL, REPORT, ODD, true>(a, x, y, idx, o, r, m, d, prev, v);
+        fast_load<S, ODD, true, FLAT>(a, idx, o, r, m, d);
+        fast_finish<S, COLL, REPORT, ODD, true, FLAT>(a, x, y, idx, o, r, m, d, prev, v);
       }
     }
   }
@@ -1068,7 +1083,9 @@ step_kernel(const __grid_constant__ StepArgs<S> a) {
   constexpr int TX = tile_warps_x<S>(), TY = BY / TX;
   const int wx = (int)threadIdx.y % TX, wy = (int)threadIdx.y / TX;
   const int x0 = ((int)blockIdx.x * TX + wx) * BX;
-  cell_step<S, COLL, REPORT, ODD>(a, x0, x0 + (int)threadIdx.x, (int)blockIdx.y * TY + wy, (int)blockIdx.z);
+  const int x = x0 + (int)threadIdx.x, y = (int)blockIdx.y * TY + wy, z = (int)blockIdx.z;
+  if (a.flat) cell_step<S, COLL, REPORT, ODD, true>(a, x0, x, y, z);
+  else cell_step<S, COLL, REPORT, ODD, false>(a, x0, x, y, z);
 }
 
 // Link masks of the warps within the obstacle's reach, one warp per 32 cells.

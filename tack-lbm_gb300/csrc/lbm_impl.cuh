@@ -18,6 +18,9 @@ StepArgs<S> make_args(const Ctx &c) {
   StepArgs<S> a{};
   S *F = static_cast<S *>(c.F);
   for (int q = 0; q < Q; ++q) a.slot[q] = F + (size_t)q * (size_t)c.n;
+  a.F = F;
+  a.n = (uint32_t)c.n;
+  a.flat = 19 * c.n <= (int64_t)UINT32_MAX && !(g.flags & LBM_FLAG_SLOT_POINTERS);
   a.nx = g.nx;
   a.ny = g.ny;
   a.nz = g.nz;

@@ -19,6 +19,7 @@ F32, F16, BF16, F64 = 0, 1, 2, 3
 HOST, DEVICE = 0, 1
 FLAG_SIMT = 1
 FLAG_BULKCOPY = 2
+FLAG_SLOT_POINTERS = 4
 FIELDS = ("ux", "uy", "uz", "p", "vmag", "r_rho", "r_ux", "r_uy", "r_uz", "r_ke", "fx", "fy", "fz")
 MONITORS = ("continuity", "momentum_x", "momentum_y", "momentum_z", "energy", "drag", "lift")
 STORAGE = {"f32": F32, "f16": F16, "bf16": BF16, "f64": F64}

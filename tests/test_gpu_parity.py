@@ -125,9 +125,10 @@ def test_trt_ref_through_kernel_entry(G):
     assert O.weight_err(out, z["ref"]) <= 2e-6           # trt_ref uses exact weights
 
 
-# step kernels: the per-cell kernel (default) and the bulk-copy staged kernel
-PATHS = [0, N.FLAG_BULKCOPY]
-PATH_IDS = ["percell", "bulkcopy"]
+# step kernels: the per-cell kernel (default), the same with the slot-pointer
+# addressing of lattices with 19 n >= 2^32 cells, and the bulk-copy staged kernel
+PATHS = [0, N.FLAG_SLOT_POINTERS, N.FLAG_BULKCOPY]
+PATH_IDS = ["percell", "slotptr", "bulkcopy"]
 
 
 @pytest.mark.parametrize("kernel", PATHS, ids=PATH_IDS)
