@@ -432,9 +432,14 @@ def row_fsi(device, peak, torch):
 
 
 def row_derived(device, peak, torch, solver):
-    """Velocity gradient, then |curl u| and Q at cell centres, on the cylinder
-    run's stride-2 output grid (256 x 128 x 32): 12 B read and 36 B written
-    per point, then 36 B read and 8 B written per cell."""
+    """The default derived fields (|curl u| and Q at cell centres) on the
+    cylinder run's stride-2 output grid (256 x 128 x 32), as DerivedFields.
+    evaluate() computes them: one lbm_vorticity_q_direct pass reading the
+    velocity (12 B per point) and writing both fields (8 B per cell). The
+    velocity gradient alone (lbm_velocity_gradient: 12 B read, 36 B written
+    per point) and the earlier two-pass path (gradient, then the fields from
+    it: + 36 B read per cell) are timed beside it. The 12 MB velocity grid sits
+    in the 129 MB L2, so these rates are not HBM-bound figures."""
     import ctypes as C
     solver.update_output()
     mx, my, mz = solver.out_dims
@@ -445,25 +450,36 @@ def row_derived(device, peak, torch, solver):
     q = torch.empty(cells, dtype=torch.float32, device=dev)
     inv_h = solver.diameter / solver.stride
 
-    def derive():
+    def direct():
+        solver._h.call("lbm_vorticity_q_direct", float(inv_h), C.c_void_p(vort.data_ptr()),
+                       C.c_void_p(q.data_ptr()), 1, None)
+
+    def gradient():
         solver._h.call("lbm_velocity_gradient", C.c_void_p(jac.data_ptr()), float(inv_h), None)
+
+    def two_pass():
+        gradient()
         solver._h.call("lbm_vorticity_q", C.c_void_p(jac.data_ptr()), C.c_void_p(vort.data_ptr()),
                        C.c_void_p(q.data_ptr()), 1, None)
 
-    for _ in range(3):
-        derive()
-    a, b = _events(torch)
-    a.record()
-    reps = 50
-    for _ in range(reps):
-        derive()
-    b.record()
-    b.synchronize()
-    per = a.elapsed_time(b) / reps
-    byts = pts * (12 + 36) + cells * (36 + 8)
-    return {"workload": f"velocity gradient + vorticity + Q at cells, {mx}x{my}x{mz} output grid",
+    def timed(fn, reps=50):
+        for _ in range(3):
+            fn()
+        a, b = _events(torch)
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        b.synchronize()
+        return a.elapsed_time(b) / reps
+
+    per, per_grad, per_two = timed(direct), timed(gradient), timed(two_pass)
+    byts = pts * 12 + cells * 8
+    return {"workload": f"vorticity + Q at cells from the velocity, {mx}x{my}x{mz} output grid",
             "ms_per_call": per, "bytes": byts, "achieved_gbs": byts / (per * 1e-3) / 1e9,
-            "frac": byts / (per * 1e-3) / 1e9 / peak}
+            "frac": byts / (per * 1e-3) / 1e9 / peak,
+            "gradient_ms": per_grad, "gradient_bytes": pts * (12 + 36),
+            "two_pass_ms": per_two}
 
 
 def next_rows(device, peak, torch, solver, rows=NEXT_ROWS):

@@ -214,6 +214,14 @@ lbm_status lbm_velocity_gradient(lbm_solver *s, float *jac, double inv_h, void *
 lbm_status lbm_vorticity_q(lbm_solver *s, const float *jac, float *vorticity, float *q, int32_t at_cells,
                            void *stream);
 
+/* The same two fields straight from the output grid's velocity, with no
+ * gradient buffer: the gradient of lbm_velocity_gradient (inv_h as there) is
+ * formed where it is used, so the results equal lbm_velocity_gradient
+ * followed by lbm_vorticity_q bit for bit (derived.py:27-30, 52-89).
+ * Either output may be NULL. */
+lbm_status lbm_vorticity_q_direct(lbm_solver *s, double inv_h, float *vorticity, float *q, int32_t at_cells,
+                                  void *stream);
+
 /* Overwrite one diagnostic field from a buffer of n floats (host or managed). */
 lbm_status lbm_set_field(lbm_solver *s, int32_t id, const float *host);
 

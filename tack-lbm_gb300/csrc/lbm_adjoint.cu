@@ -201,20 +201,26 @@ __device__ __forceinline__ T dfeq(T drho, T rho, T ux, T uy, T uz, T usq) {
   return T(wq(q)) * (drho + rho * (T(3) * s + T(4.5) * s * s - T(1.5) * usq));
 }
 
-// transposed Jacobian of feq(rho, u) applied to e[]: adds to rb and ub
+// transposed Jacobian of feq(rho, u) applied to e[]: adds to rb and ub.
+// By direction pairs (q, opp q = q + 1), with s_opp = -s_q and c_opp = -c_q:
+// a pair adds w (e_q + e_opp) to the sums of w e and w e s^2 terms, and
+// w (e_q - e_opp) to those of w e c and w e s.
 template <typename T>
 __device__ __forceinline__ void feq_vjp(const T e[Q], T rho, T ux, T uy, T uz, T &rb, T &ubx, T &uby, T &ubz) {
   const T usq = ux * ux + uy * uy + uz * uz;
-  T a0 = 0, a1x = 0, a1y = 0, a1z = 0, a2x = 0, a2y = 0, a2z = 0, q0 = 0;
-  static_for<Q>([&](auto qc) {
-    constexpr int q = decltype(qc)::value;
+  T a0 = T(wq(0)) * e[0], a1x = 0, a1y = 0, a1z = 0, a2x = 0, a2y = 0, a2z = 0, q0 = 0;
+  static_for<9>([&](auto kc) {
+    constexpr int k = decltype(kc)::value;
+    constexpr int q = pq(k);
     const T s = cdot<T, q>(ux, uy, uz);
-    const T we = T(wq(q)) * e[q];
-    a0 += we;
-    q0 += we * (T(3) * s + T(4.5) * s * s);
-    if (cx(q)) { a1x += T(cx(q)) * we; a2x += T(cx(q)) * we * s; }
-    if (cy(q)) { a1y += T(cy(q)) * we; a2y += T(cy(q)) * we * s; }
-    if (cz(q)) { a1z += T(cz(q)) * we; a2z += T(cz(q)) * we * s; }
+    const T wp = T(wq(q)) * (e[q] + e[q + 1]);
+    const T wm = T(wq(q)) * (e[q] - e[q + 1]);
+    a0 += wp;
+    q0 += T(3) * s * wm + T(4.5) * s * s * wp;
+    const T sp = s * wp;
+    if (cx(q)) { a1x += T(cx(q)) * wm; a2x += T(cx(q)) * sp; }
+    if (cy(q)) { a1y += T(cy(q)) * wm; a2y += T(cy(q)) * sp; }
+    if (cz(q)) { a1z += T(cz(q)) * wm; a2z += T(cz(q)) * sp; }
   });
   rb += a0 + q0 - T(1.5) * usq * a0;
   ubx += rho * (T(3) * a1x + T(9) * a2x - T(3) * ux * a0);
@@ -433,9 +439,12 @@ __device__ __forceinline__ void adjoint_cell(const DArgs<T> &a, int x, int idx, 
     pib[4] = T(2) * s * F.pi[4];
     pib[5] = T(2) * s * F.pi[5];
   }
-  // ne = g - feq: gb = alpha ob + sum_ab c_a c_b pib_ab, and feq's adjoint is -gb
-  static_for<Q>([&](auto qc) {
-    constexpr int q = decltype(qc)::value;
+  // ne = g - feq: gb = alpha ob + sum_ab c_a c_b pib_ab, and feq's adjoint is
+  // -gb; c_a c_b is the same for q and opp q, so each pair forms it once
+  ob[0] = alpha * ob[0];
+  static_for<9>([&](auto kc) {
+    constexpr int k = decltype(kc)::value;
+    constexpr int q = pq(k);
     T m = 0;
     if (cx(q)) m += pib[0];
     if (cy(q)) m += pib[1];
@@ -444,6 +453,7 @@ __device__ __forceinline__ void adjoint_cell(const DArgs<T> &a, int x, int idx, 
     if (cx(q) && cz(q)) m += T(cx(q) * cz(q)) * pib[4];
     if (cy(q) && cz(q)) m += T(cy(q) * cz(q)) * pib[5];
     ob[q] = alpha * ob[q] + m;
+    ob[q + 1] = alpha * ob[q + 1] + m;
   });
   {
     T r = 0, bx = 0, by = 0, bz = 0;
@@ -457,11 +467,17 @@ __device__ __forceinline__ void adjoint_cell(const DArgs<T> &a, int x, int idx, 
   const T jxb = uxb * F.fl * F.inv, jyb = uyb * F.fl * F.inv, jzb = uzb * F.fl * F.inv;
   rhob -= (uxb * F.ux + uyb * F.uy + uzb * F.uz) * F.inv;
   flb += (uxb * F.jx + uyb * F.jy + uzb * F.jz) * F.inv;
-  // moments, streaming and bounce-back (and the drag); outputs
+  // moments, streaming and bounce-back (and the drag); outputs. The
+  // momentum part c_q . jb is formed once per pair (c_opp = -c_q).
+  T cj[9];
+  static_for<9>([&](auto kc) {
+    constexpr int k = decltype(kc)::value;
+    cj[k] = cdot<T, pq(k)>(jxb, jyb, jzb);
+  });
   T rb = 0;
   static_for<Q>([&](auto qc) {
     constexpr int q = decltype(qc)::value;
-    const T gq = ob[q] + rhob + T(cx(q)) * jxb + T(cy(q)) * jyb + T(cz(q)) * jzb;
+    const T gq = q == 0 ? ob[0] + rhob : (q & 1) ? (ob[q] + rhob) + cj[(q - 1) / 2] : (ob[q] + rhob) - cj[(q - 1) / 2];
     if (!BAND || q == 0) {
       a.Go[q * a.n + idx] = gq;
     } else {

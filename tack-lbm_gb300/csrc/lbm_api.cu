@@ -1085,6 +1085,16 @@ lbm_status lbm_vorticity_q(lbm_solver *s, const float *jac, float *vorticity, fl
   return LBM_OK;
 }
 
+lbm_status lbm_vorticity_q_direct(lbm_solver *s, double inv_h, float *vorticity, float *q, int32_t at_cells,
+                                  void *stream) {
+  lbmh::Range range_("lbm_vorticity_q_direct");
+  LBM_HANDLE(s);
+  if (!std::isfinite(inv_h)) return fail(LBM_ERR_ARG, "inv_h must be finite");
+  if (at_cells != 0 && at_cells != 1) return fail(LBM_ERR_ARG, "at_cells must be 0 or 1");
+  LBM_CUDA(lbmh::launch_vortq_direct(s->c, (float)inv_h, vorticity, q, at_cells, (cudaStream_t)stream));
+  return LBM_OK;
+}
+
 lbm_status lbm_run_timed(lbm_solver *s, int32_t count, int32_t report_last, void *stream, double *ms) {
   lbmh::Range range_("lbm_run_timed");
   LBM_HANDLE(s);

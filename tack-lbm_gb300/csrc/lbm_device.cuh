@@ -1034,9 +1034,15 @@ __device__ __forceinline__ bool lid_row(const StepArgs<S> &a, int y) {
 #ifndef LBM_STEP_MIN_BLOCKS_64
 #define LBM_STEP_MIN_BLOCKS_64 5
 #endif
-template <typename S>
+// Report steps (13 more field streams and the residuals live) may take their own.
+#ifndef LBM_STEP_MIN_BLOCKS_REPORT
+#define LBM_STEP_MIN_BLOCKS_REPORT 0
+#endif
+template <typename S, bool REPORT = false>
 __host__ __device__ constexpr int step_min_blocks() {
-  return sizeof(S) == 2 ? LBM_STEP_MIN_BLOCKS_16 : sizeof(S) == 8 ? LBM_STEP_MIN_BLOCKS_64 : LBM_STEP_MIN_BLOCKS;
+  return REPORT && LBM_STEP_MIN_BLOCKS_REPORT > 0 && sizeof(S) == 4
+             ? LBM_STEP_MIN_BLOCKS_REPORT
+             : sizeof(S) == 2 ? LBM_STEP_MIN_BLOCKS_16 : sizeof(S) == 8 ? LBM_STEP_MIN_BLOCKS_64 : LBM_STEP_MIN_BLOCKS;
 }
 
 // One cell of the per-cell kernels: the warp is the 32-cell row segment at x0.
@@ -1078,7 +1084,7 @@ __host__ __device__ constexpr int tile_warps_x() {
 }
 
 template <typename S, int COLL, bool REPORT, bool ODD>
-__global__ void __launch_bounds__(BX * BY, step_min_blocks<S>())
+__global__ void __launch_bounds__(BX * BY, (step_min_blocks<S, REPORT>()))
 step_kernel(const __grid_constant__ StepArgs<S> a) {
   constexpr int TX = tile_warps_x<S>(), TY = BY / TX;
   const int wx = (int)threadIdx.y % TX, wy = (int)threadIdx.y / TX;

@@ -112,6 +112,7 @@ cudaError_t launch_coarsen(const Ctx &c, cudaStream_t st);
 cudaError_t launch_heat(const Ctx &c, bool report, cudaStream_t st);
 cudaError_t launch_jacobian(const Ctx &c, float *jac, float inv_h, cudaStream_t st);
 cudaError_t launch_vortq(const Ctx &c, const float *jac, float *vort, float *q, int at_cells, cudaStream_t st);
+cudaError_t launch_vortq_direct(const Ctx &c, float inv_h, float *vort, float *q, int at_cells, cudaStream_t st);
 // the full-resolution field output k shows (fld[k], or the temperature)
 inline float *output_source(const Ctx &c, int k) { return k < 5 ? c.fld[k] : c.heat_fld[LBM_TEMP]; }
 

@@ -74,16 +74,21 @@ class DerivedFields:
         return self.jacobian.numpy[: 9 * self.n].reshape(self.n, 3, 3)
 
     def evaluate(self):
-        """{name: (values, 'vertex' or 'element')} for the current output arrays (derived.py:204-219)."""
-        self.gradient()
+        """{name: (values, 'vertex' or 'element')} for the current output arrays (derived.py:204-219).
+        Both fields of one association come from one pass over the velocity
+        (lbm_vorticity_q_direct), with no gradient buffer in between."""
         h = self.solver._h
+        done = {}
         results = {}
         for name, (expr, at) in self.specs.items():
             cells = at == "cells"
             m = self.ncells if cells else self.n
-            h.call("lbm_vorticity_q", ctypes.c_void_p(self.jacobian.ptr), ctypes.c_void_p(self._vort.ptr),
-                   ctypes.c_void_p(self._q.ptr), int(cells), None)
-            h.call("lbm_sync")
-            src = self._vort if _KNOWN[expr.replace(" ", "")] == "vorticity" else self._q
-            results[name] = (src.numpy[:m].copy(), "element" if cells else "vertex")
+            if at not in done:
+                h.call("lbm_vorticity_q_direct", float(self.inv_h), ctypes.c_void_p(self._vort.ptr),
+                       ctypes.c_void_p(self._q.ptr), int(cells), None)
+                h.call("lbm_sync")
+                done[at] = (self._vort.numpy[:m].copy(), self._q.numpy[:m].copy())
+            vort, q = done[at]
+            src = vort if _KNOWN[expr.replace(" ", "")] == "vorticity" else q
+            results[name] = (src, "element" if cells else "vertex")
         return results

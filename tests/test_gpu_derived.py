@@ -72,3 +72,31 @@ def test_derived_gradient_against_reference_golden(case):
     want = case["jacobian"]
     tol = 4 * 2.0 ** -24 * np.abs(want) + 1e-9 * np.abs(want).max()
     assert (np.abs(g - want) <= tol).all(), np.abs(g - want).max()
+
+
+@pytest.mark.parametrize("cells", [0, 1])
+def test_direct_vorticity_q_equals_gradient_path(cells):
+    """lbm_vorticity_q_direct (no gradient buffer) gives the same floats as
+    lbm_velocity_gradient followed by lbm_vorticity_q, on an odd-sized output
+    grid (one-sided faces on every axis)."""
+    import lbm
+    s = lbm.Solver(42, 22, 10, collision="les", obstacle="sphere", reynolds=150.0, u0=0.07,
+                   diameter=6.0, stride=1, init="random", seed=5, rho_sigma=0.0, u_noise=0.02)
+    for _ in range(6):
+        s.step()
+    s.step(report=True)
+    s.monitors(7)
+    mx, my, mz = s.out_dims
+    n = mx * my * mz
+    m = (mx - 1) * (my - 1) * (mz - 1) if cells else n
+    inv_h = s.diameter / s.stride
+    jac, v1, q1, v2, q2 = (lbm.ManagedArray(k) for k in (9 * n, m, m, m, m))
+    h = s._h
+    h.call("lbm_velocity_gradient", ctypes.c_void_p(jac.ptr), float(inv_h), None)
+    h.call("lbm_vorticity_q", ctypes.c_void_p(jac.ptr), ctypes.c_void_p(v1.ptr), ctypes.c_void_p(q1.ptr),
+           cells, None)
+    h.call("lbm_vorticity_q_direct", float(inv_h), ctypes.c_void_p(v2.ptr), ctypes.c_void_p(q2.ptr), cells, None)
+    h.call("lbm_sync")
+    assert np.array_equal(v1.numpy, v2.numpy)
+    assert np.array_equal(q1.numpy, q2.numpy)
+    assert np.abs(v2.numpy).max() > 0
