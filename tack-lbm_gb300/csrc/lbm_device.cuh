@@ -717,10 +717,11 @@ __device__ __forceinline__ Offsets<S> cell_offsets(const StepArgs<S> &a, int x, 
 // the whole collision. opaque_store<S>() forms the store addresses again from
 // copies of the cell index and offsets the compiler cannot identify with the
 // originals, which keeps 7 integers live instead. That frees the registers
-// for more FP32 blocks per SM (below); the 2-byte storages, which sit at 72
-// registers either way, ran 2 % slower with it, and FP64 does not use it.
+// for more blocks per SM (below): FP32 8 blocks, FP16/BF16 8 blocks (at 7
+// blocks the 2-byte kernels ran 3 % slower with it, at 8 6 % faster than the
+// 7 blocks without it). FP64 does not use it.
 #ifndef LBM_OPAQUE_STORE_16
-#define LBM_OPAQUE_STORE_16 0
+#define LBM_OPAQUE_STORE_16 1
 #endif
 #ifndef LBM_OPAQUE_STORE_32
 #define LBM_OPAQUE_STORE_32 1
@@ -1022,14 +1023,15 @@ __device__ __forceinline__ bool lid_row(const StepArgs<S> &a, int y) {
 // (opaque_store): 0.203 ms per C2 launch, against 0.206 at 7 blocks,
 // 0.223-0.230 at 6 and 0.225 at 5 (the earlier 5 blocks without
 // opaque_store). FP16/BF16 are latency-bound with half the bytes in flight
-// per warp: 7 blocks (28 warps, 72 registers) ran 9 % faster than 5 despite
-// spills to L1 (6: 3 %, 8: 7-11 %, 10: 3 %). FP64 (the oracle-precision
-// runs, twice the registers per value) keeps 5.
+// per warp: with opaque_store and the flat slot offsets 8 blocks (32 warps,
+// 64 registers) run 0.157 ms per C2 launch against 0.162 at 7; without
+// opaque_store 7 blocks were best (0.167; 8: 0.186). FP64 (the oracle-
+// precision runs, twice the registers per value) keeps 5.
 #ifndef LBM_STEP_MIN_BLOCKS
 #define LBM_STEP_MIN_BLOCKS 8
 #endif
 #ifndef LBM_STEP_MIN_BLOCKS_16
-#define LBM_STEP_MIN_BLOCKS_16 7
+#define LBM_STEP_MIN_BLOCKS_16 8
 #endif
 #ifndef LBM_STEP_MIN_BLOCKS_64
 #define LBM_STEP_MIN_BLOCKS_64 5
