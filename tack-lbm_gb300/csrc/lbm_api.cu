@@ -658,6 +658,7 @@ lbm_status lbm_run(lbm_solver *s, int32_t count, int32_t report_last, void *stre
 static lbm_status check_kernel_error(lbm_solver *s) {
   unsigned int flag = 0;
   LBM_CUDA(cudaDeviceSynchronize());
+  if (!s->c.use_stream) return LBM_OK;  // only the bulk-copy kernel sets the flag
   LBM_CUDA(cudaMemcpy(&flag, s->c.error, sizeof(flag), cudaMemcpyDeviceToHost));
   if (flag) {
     cudaMemset(s->c.error, 0, sizeof(flag));

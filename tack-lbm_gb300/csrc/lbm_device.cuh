@@ -486,9 +486,26 @@ __device__ __forceinline__ T collide(T v[Q], const Moments<T> &m, const Pairs<T>
   return tau;
 }
 
+// v <- feq(e1, u1) + keep (v - feq(e0, u0)), both equilibria formed pair by
+// pair as they are used (no 19-value equilibrium arrays stay live).
+template <typename T>
+__device__ __forceinline__ void blend_eq(T v[Q], const EqBase<T> &e0, T ux0, T uy0, T uz0, const EqBase<T> &e1,
+                                         T ux1, T uy1, T uz1, T keep) {
+  v[0] = T(wq(0)) * e1.base + keep * (v[0] - T(wq(0)) * e0.base);
+  static_for<9>([&](auto kc) {
+    constexpr int k = decltype(kc)::value;
+    constexpr int q = pq(k);
+    const T w = T(wq(q));
+    T A0, B0, A1, B1;
+    eq_pair<T, k>(e0, ux0, uy0, uz0, A0, B0);
+    eq_pair<T, k>(e1, ux1, uy1, uz1, A1, B1);
+    v[q] = w * (A1 + B1) + keep * (v[q] - w * (A0 + B0));
+    v[q + 1] = w * (A1 - B1) + keep * (v[q + 1] - w * (A0 - B0));
+  });
+}
+
 // Sponge blend toward (1, u0*fluid, 0, 0) (lbm.py:446-456):
 // out = feq(rho_s, u_s) + (1 - sigma)(post - feq(rho, u)), in values.
-// The two equilibria are formed pair by pair as they are used.
 template <typename T, bool DEV>
 __device__ __forceinline__ void sponge(T v[Q], const Moments<T> &m, T sigma, T u0fluid) {
   const EqBase<T> e0 = eq_base<T>(rv_of<T, DEV>(m), m.rho, m.ux, m.uy, m.uz);
@@ -498,18 +515,7 @@ __device__ __forceinline__ void sponge(T v[Q], const Moments<T> &m, T sigma, T u
   const T uy_s = (T(1) - sigma) * m.uy;
   const T uz_s = (T(1) - sigma) * m.uz;
   const EqBase<T> e1 = eq_base<T>(DEV ? drho_s : rho_s, rho_s, ux_s, uy_s, uz_s);
-  const T keep = T(1) - sigma;
-  v[0] = T(wq(0)) * e1.base + keep * (v[0] - T(wq(0)) * e0.base);
-  static_for<9>([&](auto kc) {
-    constexpr int k = decltype(kc)::value;
-    constexpr int q = pq(k);
-    const T w = T(wq(q));
-    T A0, B0, A1, B1;
-    eq_pair<T, k>(e0, m.ux, m.uy, m.uz, A0, B0);
-    eq_pair<T, k>(e1, ux_s, uy_s, uz_s, A1, B1);
-    v[q] = w * (A1 + B1) + keep * (v[q] - w * (A0 + B0));
-    v[q + 1] = w * (A1 - B1) + keep * (v[q + 1] - w * (A0 - B0));
-  });
+  blend_eq<T>(v, e0, m.ux, m.uy, m.uz, e1, ux_s, uy_s, uz_s, T(1) - sigma);
 }
 
 // ---------------------------------------------------------------------------

@@ -152,8 +152,19 @@ __device__ __forceinline__ bool block_near_wing(const FsiArgs &a, int z) {
   return near;
 }
 
+// Resident blocks per SM of the FSI step (0: the compiler's choice, 80-90
+// registers; 6, 7 and 8 blocks measured no faster on the 256x128x104 wing).
+#ifndef LBM_FSI_MIN_BLOCKS
+#define LBM_FSI_MIN_BLOCKS 0
+#endif
+#if LBM_FSI_MIN_BLOCKS > 0
+#define LBM_FSI_BOUNDS __launch_bounds__(BX * BY, LBM_FSI_MIN_BLOCKS)
+#else
+#define LBM_FSI_BOUNDS __launch_bounds__(BX * BY)
+#endif
+
 template <int COLL, bool REPORT>
-__global__ void __launch_bounds__(BX * BY) fsi_step_kernel(const __grid_constant__ FsiArgs a) {
+__global__ void LBM_FSI_BOUNDS fsi_step_kernel(const __grid_constant__ FsiArgs a) {
   const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
   const bool near = block_near_wing(a, z);
   float fx = 0.f, fy = 0.f, mz = 0.f;
@@ -220,12 +231,8 @@ __global__ void __launch_bounds__(BX * BY) fsi_step_kernel(const __grid_constant
       const float wy = k.y - k.z * ((float)x - a.x_eaf);
       const float rho_s = mo.rho + sigma * (1.f - mo.rho);
       const float usx = here ? wx : mo.ux, usy = here ? wy : mo.uy, usz = here ? 0.f : mo.uz;
-      float e0[Q], e1[Q];
-      feq_val<float, false>(mo.rho, mo.rho, mo.ux, mo.uy, mo.uz, e0);
-      feq_val<float, false>(rho_s, rho_s, usx, usy, usz, e1);
-      const float keep = 1.f - sigma;
-#pragma unroll
-      for (int q = 0; q < Q; ++q) post[q] = e1[q] + keep * (post[q] - e0[q]);
+      blend_eq<float>(post, eq_base<float>(mo.rho, mo.rho, mo.ux, mo.uy, mo.uz), mo.ux, mo.uy, mo.uz,
+                      eq_base<float>(rho_s, rho_s, usx, usy, usz), usx, usy, usz, 1.f - sigma);
     }
 #pragma unroll
     for (int q = 0; q < Q; ++q) __stcs(a.fout + (size_t)q * a.n + idx, post[q]);

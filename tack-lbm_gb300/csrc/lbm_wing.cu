@@ -121,12 +121,8 @@ __global__ void __launch_bounds__(BX * BY) wing_step_kernel(const __grid_constan
       const float rho_s = mo.rho + sigma * (1.f - mo.rho);
       const float usx = mo.ux + sigma * (tx - mo.ux), usy = mo.uy + sigma * (ty - mo.uy),
                   usz = (1.f - sigma) * mo.uz;
-      float e0[Q], e1[Q];
-      feq_val<float, false>(mo.rho, mo.rho, mo.ux, mo.uy, mo.uz, e0);
-      feq_val<float, false>(rho_s, rho_s, usx, usy, usz, e1);
-      const float keep = 1.f - sigma;
-#pragma unroll
-      for (int q = 0; q < Q; ++q) post[q] = e1[q] + keep * (post[q] - e0[q]);
+      blend_eq<float>(post, eq_base<float>(mo.rho, mo.rho, mo.ux, mo.uy, mo.uz), mo.ux, mo.uy, mo.uz,
+                      eq_base<float>(rho_s, rho_s, usx, usy, usz), usx, usy, usz, 1.f - sigma);
     }
 #pragma unroll
     for (int q = 0; q < Q; ++q) __stcs(a.fout + (size_t)q * a.n + idx, post[q]);
