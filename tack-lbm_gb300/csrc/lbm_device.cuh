@@ -355,17 +355,22 @@ __device__ __forceinline__ Moments<T> moments(const T v[Q], bool fluid, Pairs<T>
   return m;
 }
 
+// c_q . u of the pair's first direction q = pq(k): its first nonzero
+// component is +1 and it has at most one more (no addition of a zero)
 template <typename T, int k>
 __device__ __forceinline__ T pair_dot(T ux, T uy, T uz) {
   constexpr int q = pq(k);
-  T s = T(0);
-  if (cx(q) == 1) s += ux;
-  if (cx(q) == -1) s -= ux;
-  if (cy(q) == 1) s += uy;
-  if (cy(q) == -1) s -= uy;
-  if (cz(q) == 1) s += uz;
-  if (cz(q) == -1) s -= uz;
-  return s;
+  static_assert(cx(q) == 1 || (cx(q) == 0 && (cy(q) == 1 || (cy(q) == 0 && cz(q) == 1))), "pair order");
+  if constexpr (cx(q) == 1) {
+    if constexpr (cy(q) != 0) return cy(q) == 1 ? ux + uy : ux - uy;
+    if constexpr (cz(q) != 0) return cz(q) == 1 ? ux + uz : ux - uz;
+    return ux;
+  } else if constexpr (cy(q) == 1) {
+    if constexpr (cz(q) != 0) return cz(q) == 1 ? uy + uz : uy - uz;
+    return uy;
+  } else {
+    return uz;
+  }
 }
 
 // A and B of every pair (see above) and the rest population's equilibrium
@@ -828,7 +833,8 @@ __device__ __forceinline__ Moments<typename Store<S>::T> fluid_update(const Step
   Pairs<T> pr;
   const Moments<T> mo = moments<T, DEV>(d, true, pr);
   const T tau = collide<T, COLL, DEV>(d, mo, pr, a.omega_bgk, a.tau0, a.smag_c, a.magic);
-  if (a.aux) a.aux[idx] = make_float4((float)mo.ux, (float)mo.uy, (float)mo.uz, (float)tau);
+  // the temperature coupling (FP32 storage only)
+  if (sizeof(S) == 4 && a.aux) a.aux[idx] = make_float4((float)mo.ux, (float)mo.uy, (float)mo.uz, (float)tau);
   const T t = fmax(T(0), (T(x) - a.sponge_start) * a.inv_sponge_len);
   const T sigma = a.sponge_strength * t * t;
   if (sigma != T(0)) sponge<T, DEV>(d, mo, sigma, a.u0);
