@@ -422,23 +422,28 @@ __device__ __forceinline__ T rv_of(const Moments<T> &m) {
   return DEV ? m.drho : m.rho;
 }
 
-// v <- v + om (feq - v), written v (1 - om) + om feq: with om w A and om w B
-// formed once per pair that is one fused multiply-add per population. The
-// pairs' A and B are formed as each pair is relaxed.
+// v <- v + om (feq - v), written v (1 - om) + om feq. With feq = w (A +- B),
+// A = base + 4.5 rho s^2 and B = 3 rho s, om w feq = X +- Y for
+// X = om w base + (om w 4.5 rho) s^2 and Y = (om w 3 rho) s: the three
+// coefficients are formed once per weight class, then each population is
+// (v keep + X) +- Y, two fused multiply-adds. (Against om w A and om w B
+// formed per pair: 3.6 % faster FP16 and 1.5 % faster FP32 C2 launches.)
 template <typename T>
 __device__ __forceinline__ void relax_bgk(T v[Q], T om, const EqBase<T> &e, T ux, T uy, T uz) {
   const T keep = T(1) - om;
   const T om1 = om * T(wq(1)), om7 = om * T(wq(7));
   v[0] = v[0] * keep + om * (T(wq(0)) * e.base);
+  const T ob1 = om1 * e.base, ob7 = om7 * e.base;
+  const T o451 = om1 * e.r45, o457 = om7 * e.r45;
+  const T o31 = om1 * e.r3, o37 = om7 * e.r3;
   static_for<9>([&](auto kc) {
     constexpr int k = decltype(kc)::value;
     constexpr int q = pq(k);
-    T A, B;
-    eq_pair<T, k>(e, ux, uy, uz, A, B);
-    const T ow = k < 3 ? om1 : om7;
-    const T oA = ow * A, oB = ow * B;
-    v[q] = v[q] * keep + (oA + oB);
-    v[q + 1] = v[q + 1] * keep + (oA - oB);
+    const T sd = pair_dot<T, k>(ux, uy, uz);
+    const T X = fma((k < 3 ? o451 : o457) * sd, sd, k < 3 ? ob1 : ob7);
+    const T o3 = k < 3 ? o31 : o37;
+    v[q] = fma(o3, sd, fma(v[q], keep, X));
+    v[q + 1] = fma(-o3, sd, fma(v[q + 1], keep, X));
   });
 }
 
@@ -460,9 +465,11 @@ __device__ __forceinline__ T collide(T v[Q], const Moments<T> &m, const Pairs<T>
   const T iso = T(W2) * (m.drho - T(1.5) * m.rho * usq) + r45 * T(W22) * usq;
   const T diag = r45 * T(W2 - W22);
   const T offd = T(9) * m.rho * T(W22);
-  const T pxx = (pr.D[0] + pr.D[3] + pr.D[4] + pr.D[5] + pr.D[6]) - iso - diag * uxx;
-  const T pyy = (pr.D[1] + pr.D[3] + pr.D[4] + pr.D[7] + pr.D[8]) - iso - diag * uyy;
-  const T pzz = (pr.D[2] + pr.D[5] + pr.D[6] + pr.D[7] + pr.D[8]) - iso - diag * uzz;
+  // the diagonal pair sums share the diagonal-direction pairs
+  const T s34 = pr.D[3] + pr.D[4], s56 = pr.D[5] + pr.D[6], s78 = pr.D[7] + pr.D[8];
+  const T pxx = ((pr.D[0] + s34) + s56) - iso - diag * uxx;
+  const T pyy = ((pr.D[1] + s34) + s78) - iso - diag * uyy;
+  const T pzz = ((pr.D[2] + s56) + s78) - iso - diag * uzz;
   const T pxy = (pr.D[3] - pr.D[4]) - offd * m.ux * m.uy;
   const T pxz = (pr.D[5] - pr.D[6]) - offd * m.ux * m.uz;
   const T pyz = (pr.D[7] - pr.D[8]) - offd * m.uy * m.uz;
