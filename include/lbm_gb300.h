@@ -107,10 +107,13 @@ typedef struct lbm_config {
  * runs. LBM_FLAG_SIMT asks for the per-cell kernel explicitly. */
 #define LBM_FLAG_SIMT 1
 #define LBM_FLAG_BULKCOPY 2
-/* LBM_FLAG_SLOT_POINTERS makes the per-cell step kernels address the 19
- * population slots through 19 pointers, as they must for lattices with
- * 19 n >= 2^32 cells; smaller lattices otherwise use 32-bit offsets from
- * one base pointer (faster). The results are the same either way. */
+/* LBM_FLAG_SLOT_POINTERS keeps the populations in 19 slot rows of n cells
+ * and makes the per-cell step kernels address them through 19 pointers, as
+ * they must for lattices with 19 n >= 2^32 cells. Smaller lattices otherwise
+ * use 32-bit offsets from one base pointer (faster), and FP32 storage keeps
+ * its populations in 32-cell blocks of 19 slots (faster again). The results
+ * are the same either way; lbm_get/set_populations always exchange the
+ * reference layout f[q*n + idx]. */
 #define LBM_FLAG_SLOT_POINTERS 4
 
 typedef struct lbm_solver lbm_solver;

@@ -455,6 +455,15 @@ lbm_status lbm_create(const lbm_config *cfg, lbm_solver **out) {
     c.nseg = c.nseg_x * cfg->ny * cfg->nz;
   }
   {
+    // population layout: blocks of 32 cells with their 19 slots side by side
+    // for the storage types that run faster so, where 32-bit offsets reach
+    const int64_t nxb = (cfg->nx + lbmk::BLK - 1) / lbmk::BLK;
+    c.npos = nxb * lbmk::BLK * cfg->ny * cfg->nz;
+    c.rowp = (uint32_t)(nxb * lbmk::Q * lbmk::BLK);
+    c.blocked = lbmk::blocked_layout((int)storage_bytes(cfg->storage)) && !c.use_stream &&
+                !(cfg->flags & LBM_FLAG_SLOT_POINTERS) && 19 * c.npos <= (int64_t)UINT32_MAX;
+  }
+  {
     cudaError_t e0 = cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, cfg->device);
     if (e0 != cudaSuccess) {
       delete s;
@@ -478,7 +487,7 @@ lbm_status lbm_create(const lbm_config *cfg, lbm_solver **out) {
     delete s;
     return e;
   };
-  const size_t fbytes = (size_t)19 * (size_t)c.n * storage_bytes(cfg->storage);
+  const size_t fbytes = (size_t)19 * (size_t)(c.blocked ? c.npos : c.n) * storage_bytes(cfg->storage);
   cudaError_t e = cudaMalloc(&c.F, fbytes);
   if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("population buffer: ") + cudaGetErrorString(e)));
   s->bytes += (int64_t)fbytes;

@@ -102,10 +102,14 @@ template <typename S> struct Store;
 template <typename S>
 struct StepArgs {
   using P = typename Store<S>::T;  // arithmetic precision of the step
-  S *slot[Q];             // slot[q] = F + q*n
-  S *F;                   // slot 0
+  S *slot[Q];             // slot[q] = F + q*n (slot layout)
+  S *F;                   // the population buffer
   uint32_t n;             // cells (the slot stride)
-  int flat;               // 19 n < 2^32: the step kernels address slots by 32-bit offsets from F
+  int flat;               // the step kernels address populations by 32-bit offsets from F
+  int blk;                // block layout (see blocked_layout)
+  uint32_t rowp;          // block layout: elements per lattice row
+  int bstep[4];           // block layout, position offsets modulo 2^32: to the cell at
+  int bwrap[4];           //   y - 1, y + 1, z - 1, z + 1, and across the periodic wraps
   int nx, ny, nz, nxy;
   Geo geo;
   int lateral, vertical;
@@ -122,6 +126,50 @@ struct StepArgs {
   const uint32_t *masks;         // link masks of the warps in the reach box (32 words each)
   int gx, gy;             // grid dimensions in blocks (x, y)
 };
+
+// Population layouts. Slot layout: slot q of cell idx at F[q n + idx]
+// (slot[q] + idx). Block layout: each lattice row is cut into 32-cell blocks
+// (the last one padded) and a block keeps its 19 slots side by side, 32
+// elements each, so slot q of the cell at (x, row) sits at
+//   (row ceil(nx / 32) + x / 32) 19 32 + 32 q + x % 32.
+// A warp (a 32-cell row segment) then finds the 19 slots of its cells at
+// fixed offsets from one base, and its 19 loads fall in one 2.4 kB stretch
+// of HBM (FP32). Storage types whose blocked_layout() holds use it wherever
+// 32-bit offsets reach (19 x the padded cells < 2^32), except under the
+// bulk-copy kernel (which streams slot rows) and LBM_FLAG_SLOT_POINTERS.
+// Measured per C2 launch: FP32 0.1973 -> 0.1931 ms (report steps 0.367 ->
+// 0.355 ms); FP16 0.1498 -> 0.1559 ms in a first form with more spills on
+// the odd step, so 2-byte storage keeps the slot layout.
+#ifndef LBM_BLOCKED_32
+#define LBM_BLOCKED_32 1
+#endif
+#ifndef LBM_BLOCKED_16
+#define LBM_BLOCKED_16 0
+#endif
+constexpr int BLK = 32;
+__host__ __device__ constexpr bool blocked_layout(int bytes) {
+  return bytes == 4 ? LBM_BLOCKED_32 != 0 : bytes == 2 ? LBM_BLOCKED_16 != 0 : false;
+}
+
+// block layout: offset of slot 0 of cell (x, row), row = z ny + y
+template <typename S>
+__device__ __forceinline__ uint32_t blk_pos(const StepArgs<S> &a, int row, int x) {
+  return (uint32_t)row * a.rowp + (uint32_t)(x >> 5) * (uint32_t)(Q * BLK) + (uint32_t)(x & (BLK - 1));
+}
+
+// slot q of cell (x, y, z), either layout (the kernels off the per-cell fast path)
+template <typename S>
+__device__ __forceinline__ S *elem(const StepArgs<S> &a, int q, int x, int y, int z) {
+  if (!a.blk) return a.slot[q] + ((z * a.ny + y) * a.nx + x);
+  return a.F + (size_t)blk_pos(a, z * a.ny + y, x) + (size_t)(q * BLK);
+}
+// slot q of cell idx = (z ny + y) nx + x
+template <typename S>
+__device__ __forceinline__ S *elem(const StepArgs<S> &a, int q, int idx) {
+  if (!a.blk) return a.slot[q] + idx;
+  const int row = idx / a.nx;
+  return a.F + (size_t)blk_pos(a, row, idx - row * a.nx) + (size_t)(q * BLK);
+}
 
 // Geometry of a configuration in the float32 form the kernels evaluate
 // (r^2 rounded like the reference's r*r).
@@ -718,9 +766,24 @@ struct Row {
 constexpr uint32_t MASK_SOLID = 1u << 19;
 constexpr uint32_t MASK_LINKS = MASK_SOLID - 1;
 
-template <typename S>
+// The six neighbour offsets of a cell in its layout's element offsets: cell
+// indices in the slot layout; in the block layout, positions (the x offsets
+// then differ at block edges, and a row is rowp elements). Block offsets are
+// formed modulo 2^32 (positions may pass 2^31), as are the sums of them.
+template <bool FLAT, typename S>
 __device__ __forceinline__ Offsets<S> cell_offsets(const StepArgs<S> &a, int x, int y, int z) {
   Offsets<S> o;
+  if (FLAT && blocked_layout(sizeof(S))) {
+    const int xm = x == 0 ? a.nx - 1 : x - 1, xq = x == a.nx - 1 ? 0 : x + 1;
+    const int bx = x >> 5, lx = x & (BLK - 1);
+    o.dxm = ((xm >> 5) - bx) * (Q * BLK) + ((xm & (BLK - 1)) - lx);
+    o.dxp = ((xq >> 5) - bx) * (Q * BLK) + ((xq & (BLK - 1)) - lx);
+    o.dym = y == 0 ? a.bwrap[0] : a.bstep[0];
+    o.dyp = y == a.ny - 1 ? a.bwrap[1] : a.bstep[1];
+    o.dzm = z == 0 ? a.bwrap[2] : a.bstep[2];
+    o.dzp = z == a.nz - 1 ? a.bwrap[3] : a.bstep[3];
+    return o;
+  }
   o.dxm = x == 0 ? a.nx - 1 : -1;
   o.dxp = x == a.nx - 1 ? 1 - a.nx : 1;
   o.dym = y == 0 ? (a.ny - 1) * a.nx : -a.nx;
@@ -770,25 +833,27 @@ __device__ __forceinline__ Row row_of(const StepArgs<S> &a, int y, int z) {
   return r;
 }
 
-// Element e of slot q. FLAT (lattices with 19 n < 2^32, which the step
-// kernels check once per launch) forms it from the one base pointer F and a
-// 32-bit element offset q n + e: two instructions, where the 19 slot
-// pointers of the other form each have to be fetched from the kernel's
-// parameter bank again (registers do not hold them all). 3-7 % faster per
-// C2 launch in FP32 and FP16.
+// Slot q at element offset e (a cell index, or a block position). FLAT
+// (lattices whose offsets fit 32 bits, which the step kernels check once per
+// launch) forms it from the one base pointer F: in the slot layout from the
+// 32-bit offset q n + e (two instructions, where the 19 slot pointers of the
+// other form each have to be fetched from the kernel's parameter bank again:
+// 3-7 % faster per C2 launch in FP32 and FP16); in the block layout q 32 is
+// a constant offset of the load or store itself.
 template <bool FLAT, typename S>
-__device__ __forceinline__ S *slot_at(const StepArgs<S> &a, int q, int e) {
-  if (FLAT) return a.F + (size_t)((uint32_t)q * a.n + (uint32_t)e);
-  return a.slot[q] + e;
+__device__ __forceinline__ S *slot_at(const StepArgs<S> &a, int q, uint32_t e) {
+  if (FLAT && blocked_layout(sizeof(S))) return a.F + (size_t)e + q * BLK;
+  if (FLAT) return a.F + (size_t)((uint32_t)q * a.n + e);
+  return a.slot[q] + (int)e;
 }
 
 // L(x, q): where population q of the cell streams from (odd steps read it there)
 template <int q, bool SPECIAL, bool FLAT, typename S>
-__device__ __forceinline__ S *src_loc(const StepArgs<S> &a, int idx, const Offsets<S> &o, const Row &r) {
+__device__ __forceinline__ S *src_loc(const StepArgs<S> &a, uint32_t idx, const Offsets<S> &o, const Row &r) {
   const int xp = cx(q) == 1 ? o.dxm : cx(q) == -1 ? o.dxp : 0;
   const int yp = cy(q) == 1 ? o.dym : cy(q) == -1 ? o.dyp : 0;
   const int zp = cz(q) == 1 ? o.dzm : cz(q) == -1 ? o.dzp : 0;
-  if (!SPECIAL) return slot_at<FLAT>(a, opp(q), idx + xp + yp + zp);
+  if (!SPECIAL) return slot_at<FLAT>(a, opp(q), idx + (uint32_t)xp + (uint32_t)yp + (uint32_t)zp);
   const bool ry = (cy(q) == 1 && r.ylo) || (cy(q) == -1 && r.yhi);
   const bool rz = (cz(q) == 1 && r.zlo) || (cz(q) == -1 && r.zhi);
   constexpr int s00 = opp(q);
@@ -796,7 +861,7 @@ __device__ __forceinline__ S *src_loc(const StepArgs<S> &a, int idx, const Offse
   constexpr int s10 = opp(dir(cx(q), -cy(q), cz(q)));
   constexpr int s11 = opp(dir(cx(q), -cy(q), -cz(q)));
   const int slot = ry ? (rz ? s11 : s10) : (rz ? s01 : s00);
-  return slot_at<FLAT>(a, slot, idx + xp + (ry ? 0 : yp) + (rz ? 0 : zp));
+  return slot_at<FLAT>(a, slot, idx + (uint32_t)xp + (uint32_t)(ry ? 0 : yp) + (uint32_t)(rz ? 0 : zp));
 }
 
 // moving-wall term 6 w_q c_q.u_w of a bounce link at its midpoint (lbm.py:417-428)
@@ -812,18 +877,18 @@ __device__ __forceinline__ typename Store<S>::T wall_term(const StepArgs<S> &a, 
 }
 
 template <typename S, bool ODD, bool SPECIAL, bool FLAT>
-__device__ __forceinline__ void fast_load(const StepArgs<S> &a, int idx, const Offsets<S> &o, const Row &r,
+__device__ __forceinline__ void fast_load(const StepArgs<S> &a, uint32_t ip, const Offsets<S> &o, const Row &r,
                                           uint32_t m, typename Store<S>::T d[Q]) {
   // (report steps load the previous fields beside this, see load_prev)
   static_for<Q>([&](auto qc) {
     constexpr int q = decltype(qc)::value;
-    S *own = slot_at<FLAT>(a, q, idx);
+    S *own = slot_at<FLAT>(a, q, ip);
     const S *addr;
     if (!SPECIAL) {
-      addr = ODD ? src_loc<q, false, FLAT>(a, idx, o, r) : own;
+      addr = ODD ? src_loc<q, false, FLAT>(a, ip, o, r) : own;
     } else {
       const bool b = (m >> q) & 1u;
-      S *src = src_loc<q, true, FLAT>(a, idx, o, r);
+      S *src = src_loc<q, true, FLAT>(a, ip, o, r);
       addr = ODD ? (b ? own : src) : (b ? src : own);
     }
     d[q] = Store<S>::template gload<q>(addr);
@@ -849,9 +914,10 @@ __device__ __forceinline__ Moments<typename Store<S>::T> fluid_update(const Step
 }
 
 // The rest of the cell's step after fast_load: bounce-back links, the update,
-// the stores and the report fields.
+// the stores and the report fields. idx indexes the fields, ip the populations.
 template <typename S, int COLL, bool REPORT, bool ODD, bool SPECIAL, bool FLAT>
-__device__ __forceinline__ void fast_finish(const StepArgs<S> &a, int x, int y, int idx, const Offsets<S> &o,
+__device__ __forceinline__ void fast_finish(const StepArgs<S> &a, int x, int y, int idx, uint32_t ip,
+                                            const Offsets<S> &o,
                                             const Row &r, uint32_t m, typename Store<S>::T d[Q], const Prev &prev,
                                             float v[NSUM]) {
   using T = typename Store<S>::T;
@@ -881,13 +947,13 @@ __device__ __forceinline__ void fast_finish(const StepArgs<S> &a, int x, int y, 
   Moments<T> mo;
   if (!here) {
     mo = fluid_update<S, COLL>(a, x, idx, d);
-    const int idx_s = opaque_store<S>() ? opaque(idx) : idx;
+    const uint32_t ip_s = opaque_store<S>() ? (uint32_t)opaque((int)ip) : ip;
     const Offsets<S> o_s = opaque_store<S>() ? opaque(o) : o;
     static_for<Q>([&](auto pc) {
       constexpr int p = decltype(pc)::value;
       // population p moves to x + c_p: the odd-step source location of direction opp(p)
-      if (ODD) Store<S>::template gstore<p>(src_loc<opp(p), SPECIAL, FLAT>(a, idx_s, o_s, r), d[p]);
-      else Store<S>::template gstore<p>(slot_at<FLAT>(a, opp(p), idx), d[p]);
+      if (ODD) Store<S>::template gstore<p>(src_loc<opp(p), SPECIAL, FLAT>(a, ip_s, o_s, r), d[p]);
+      else Store<S>::template gstore<p>(slot_at<FLAT>(a, opp(p), ip), d[p]);
     });
   } else {
     Pairs<T> pr;
@@ -937,8 +1003,7 @@ __device__ __forceinline__ Link<S> make_link(const StepArgs<S> &a, int x, int y,
   constexpr int s01 = opp(dir(cx(q), cy(q), -cz(q)));
   constexpr int s10 = opp(dir(cx(q), -cy(q), cz(q)));
   constexpr int s11 = opp(dir(cx(q), -cy(q), -cz(q)));
-  S *base = ry ? (rz ? a.slot[s11] : a.slot[s10]) : (rz ? a.slot[s01] : a.slot[s00]);
-  k.L = base + ((zs * a.ny + ys) * a.nx + xs);
+  k.L = elem(a, ry ? (rz ? s11 : s10) : (rz ? s01 : s00), xs, ys, zs);
   // moving-wall term at the link midpoint (lbm.py:417-425)
   T cu = T(0);
   if (k.lid) {
@@ -976,11 +1041,11 @@ __device__ __forceinline__ void general_cell(const StepArgs<S> &a, int x, int y,
     if (here) {
       // obstacle cell: streamed-in values, or its own w_q on its bounce links
       if (bb) val = rest_value<T, DEV>(q) + wall_term;
-      else val = ODD ? Store<S>::template gload<q>(k.L) : Store<S>::template gload<q>(a.slot[q] + idx);
+      else val = ODD ? Store<S>::template gload<q>(k.L) : Store<S>::template gload<q>(elem(a, q, x, y, z));
     } else {
       S *src;
-      if (ODD) src = bb ? a.slot[q] + idx : k.L;
-      else src = k.wall ? k.L : a.slot[q] + idx;
+      if (ODD) src = bb ? elem(a, q, x, y, z) : k.L;
+      else src = k.wall ? k.L : elem(a, q, x, y, z);
       const T got = Store<S>::template gload<q>(src);
       val = bb ? got + wall_term : got;
       if (k.wall) {
@@ -1007,9 +1072,9 @@ __device__ __forceinline__ void general_cell(const StepArgs<S> &a, int x, int y,
       S *dst;
       if (ODD) {
         const Link<S> k = make_link<S, o>(a, x, y, z, geo);
-        dst = k.lid ? a.slot[o] + idx : k.L;
+        dst = k.lid ? elem(a, o, x, y, z) : k.L;
       } else {
-        dst = a.slot[o] + idx;
+        dst = elem(a, o, x, y, z);
       }
       Store<S>::template gstore<p>(dst, d[p]);
     });
@@ -1083,18 +1148,19 @@ __device__ __forceinline__ void cell_step(const StepArgs<S> &a, int x0, int x, i
   if (y < a.ny && !lid_row(a, y) && x < a.nx) {
     const int idx = (z * a.ny + y) * a.nx + x;
     const Row r = row_of(a, y, z);
-    const Offsets<S> o = cell_offsets(a, x, y, z);
+    const Offsets<S> o = cell_offsets<FLAT>(a, x, y, z);
+    const uint32_t ip = FLAT && blocked_layout(sizeof(S)) ? blk_pos(a, z * a.ny + y, x) : (uint32_t)idx;
     T d[Q];
     Prev prev{0.f, 0.f, 0.f, 0.f};
     if (!(r.ylo || r.yhi || r.zlo || r.zhi) && !walls) {
       if (REPORT) prev = load_prev(a.fld, idx);
-      fast_load<S, ODD, false, FLAT>(a, idx, o, r, 0u, d);
-      fast_finish<S, COLL, REPORT, ODD, false, FLAT>(a, x, y, idx, o, r, 0u, d, prev, v);
+      fast_load<S, ODD, false, FLAT>(a, ip, o, r, 0u, d);
+      fast_finish<S, COLL, REPORT, ODD, false, FLAT>(a, x, y, idx, ip, o, r, 0u, d, prev, v);
     } else {
       if (REPORT || !(m & MASK_SOLID)) {
         if (REPORT) prev = load_prev(a.fld, idx);
-        fast_load<S, ODD, true, FLAT>(a, idx, o, r, m, d);
-        fast_finish<S, COLL, REPORT, ODD, true, FLAT>(a, x, y, idx, o, r, m, d, prev, v);
+        fast_load<S, ODD, true, FLAT>(a, ip, o, r, m, d);
+        fast_finish<S, COLL, REPORT, ODD, true, FLAT>(a, x, y, idx, ip, o, r, m, d, prev, v);
       }
     }
   }
@@ -1172,7 +1238,7 @@ __global__ void import_kernel(const __grid_constant__ StepArgs<S> a, const V *sr
     // even view: population q of cell idx sits in slot opp(q)
     static_for<Q>([&](auto qc) {
       constexpr int q = decltype(qc)::value;
-      Store<S>::template store_value<q>(a.slot[opp(q)] + idx, (double)src[(size_t)q * n + idx]);
+      Store<S>::template store_value<q>(elem(a, opp(q), idx), (double)src[(size_t)q * n + idx]);
     });
   }
 }
@@ -1192,10 +1258,10 @@ __global__ void export_kernel(const __grid_constant__ StepArgs<S> a, V *dst, int
       if (here) {
         v = (double)wq(q);
       } else if (odd_next) {
-        v = Store<S>::template load_value<q>(a.slot[o] + idx);
+        v = Store<S>::template load_value<q>(elem(a, o, x, y, z));
       } else {
         const Link<S> k = make_link<S, o>(a, x, y, z);
-        v = Store<S>::template load_value<q>(k.lid ? a.slot[o] + idx : k.L);
+        v = Store<S>::template load_value<q>(k.lid ? elem(a, o, x, y, z) : k.L);
       }
       dst[(size_t)q * n + idx] = (V)v;
     });
@@ -1218,7 +1284,7 @@ __global__ void init_kernel(const __grid_constant__ StepArgs<S> a, float seed_am
     feq_val<T, Store<S>::DEV>(Store<S>::DEV ? T(0) : T(1), T(1), ux, uy, T(0), eq);
     static_for<Q>([&](auto qc) {
       constexpr int q = decltype(qc)::value;
-      Store<S>::template store<q>(a.slot[opp(q)] + idx, eq[q]);
+      Store<S>::template store<q>(elem(a, opp(q), x, y, z), eq[q]);
     });
   }
 }
@@ -1257,7 +1323,7 @@ __global__ void init_random_kernel(const __grid_constant__ StepArgs<S> a, float 
     feq_val<T, Store<S>::DEV>(Store<S>::DEV ? drho : T(1) + drho, T(1) + drho, ux, uy, uz, eq);
     static_for<Q>([&](auto qc) {
       constexpr int q = decltype(qc)::value;
-      Store<S>::template store<q>(a.slot[opp(q)] + idx, eq[q]);
+      Store<S>::template store<q>(elem(a, opp(q), x, y, z), eq[q]);
     });
   }
 }

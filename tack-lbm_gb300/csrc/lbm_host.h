@@ -42,7 +42,10 @@ struct Range {
 struct Ctx {
   lbm_config cfg;
   int64_t n;                 // cells
-  void *F;                   // 19*n populations, storage precision cfg.storage
+  void *F;                   // the populations, storage precision cfg.storage
+  int blocked;               // F in the block layout (19 x npos), else the slot layout (19 x n)
+  int64_t npos;              // block layout: cells with each row padded to whole 32-cell blocks
+  uint32_t rowp;             // block layout: elements per lattice row
   float *fld[LBM_NUM_FIELDS];
   float **fld_dev;           // the field pointers in device memory (for the sums kernel)
   float2 *partials;          // 8 compensated float pairs per block (report steps)

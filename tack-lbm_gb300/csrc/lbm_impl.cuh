@@ -20,7 +20,22 @@ StepArgs<S> make_args(const Ctx &c) {
   for (int q = 0; q < Q; ++q) a.slot[q] = F + (size_t)q * (size_t)c.n;
   a.F = F;
   a.n = (uint32_t)c.n;
-  a.flat = 19 * c.n <= (int64_t)UINT32_MAX && !(g.flags & LBM_FLAG_SLOT_POINTERS);
+  a.blk = c.blocked;
+  a.rowp = c.rowp;
+  {
+    const uint32_t planep = c.rowp * (uint32_t)g.ny;
+    a.bstep[0] = (int)(0u - c.rowp);
+    a.bstep[1] = (int)c.rowp;
+    a.bstep[2] = (int)(0u - planep);
+    a.bstep[3] = (int)planep;
+    a.bwrap[0] = (int)((uint32_t)(g.ny - 1) * c.rowp);
+    a.bwrap[1] = (int)(0u - (uint32_t)(g.ny - 1) * c.rowp);
+    a.bwrap[2] = (int)((uint32_t)(g.nz - 1) * planep);
+    a.bwrap[3] = (int)(0u - (uint32_t)(g.nz - 1) * planep);
+  }
+  // a storage type with the block layout has no flat slot-layout form
+  a.flat = blocked_layout(sizeof(S)) ? c.blocked
+                                     : 19 * c.n <= (int64_t)UINT32_MAX && !(g.flags & LBM_FLAG_SLOT_POINTERS);
   a.nx = g.nx;
   a.ny = g.ny;
   a.nz = g.nz;

@@ -445,6 +445,43 @@ def test_two_byte_storage_steps_and_fields(G, case, collision, storage, tol):
         f = g
 
 
+BLOCK_CASES = {
+    # 75 cells per row: two full 32-cell blocks and one padded block of 11
+    "cylinder_slip_les": dict(nx=75, collision="les", obstacle="cylinder", ox=31.6, oy=5.4, r=3.3,
+                              omega_rot=0.04, lateral="slip", vertical="slip"),
+    "box_lid_trt": dict(nx=75, collision="trt", obstacle="box", ox=40.0, oy=6.0, oz=3.0, hx=3.0, hy=2.5,
+                        hz=2.0, lateral="lid", vertical="periodic", u_lid=0.05),
+    "sphere_periodic_bgk": dict(nx=64, collision="bgk", obstacle="sphere", ox=33.0, oy=5.5, oz=3.5, r=2.6),
+    "one_cell_rows": dict(nx=1, collision="les", obstacle="none"),
+}
+
+
+@pytest.mark.parametrize("case", list(BLOCK_CASES))
+def test_block_layout_matches_slot_layout(G, case):
+    """FP32 populations in 32-cell blocks (the default layout) and in 19 slot
+    rows (LBM_FLAG_SLOT_POINTERS) go through the same arithmetic, so seven
+    steps (two of them report steps) give bit-identical populations and
+    fields: padded blocks, wrap-around across block edges, lid rows (the
+    general kernel), masked warps."""
+    opts = dict(BLOCK_CASES[case])
+    nx = opts.pop("nx")
+    cfg = O.Config(nx, 12, 7, nu=0.02, u0=0.07, sponge_start=max(nx - 8.0, 0.0), sponge_strength=0.9, **opts)
+    hb = native_handle(cfg, "f32", flags=0)
+    hs = native_handle(cfg, "f32", flags=N.FLAG_SLOT_POINTERS)
+    for h in (hb, hs):
+        h.call("lbm_init_random", 1e-3, 0.01, 11)
+    assert np.array_equal(get(hb, cfg.n), get(hs, cfg.n))
+    for k in range(7):
+        rep = k in (3, 4)
+        for h in (hb, hs):
+            h.call("lbm_step", int(rep), None)
+        assert np.array_equal(get(hb, cfg.n), get(hs, cfg.n)), f"{case} step {k + 1}"
+        if rep:
+            fb, fs = get_fields(hb, cfg.n), get_fields(hs, cfg.n)
+            for name in O.FIELDS:
+                assert np.array_equal(fb[name], fs[name]), f"{case} step {k + 1} {name}"
+
+
 @pytest.mark.parametrize("kind", ["les_slipz", "lid_box", "heatsink_heat", "bulkcopy", "f16"])
 def test_run_graphs_match_single_steps(G, kind):
     """lbm_run launches pairs of quiet steps as CUDA graphs: the result is the
