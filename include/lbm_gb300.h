@@ -109,11 +109,12 @@ typedef struct lbm_config {
 #define LBM_FLAG_BULKCOPY 2
 /* LBM_FLAG_SLOT_POINTERS keeps the populations in 19 slot rows of n cells
  * and makes the per-cell step kernels address them through 19 pointers, as
- * they must for lattices with 19 n >= 2^32 cells. Smaller lattices otherwise
- * use 32-bit offsets from one base pointer (faster), and FP32 storage keeps
- * its populations in 32-cell blocks of 19 slots (faster again). The results
- * are the same either way; lbm_get/set_populations always exchange the
- * reference layout f[q*n + idx]. */
+ * they must when 32-bit element offsets do not reach (19 n >= 2^32).
+ * Otherwise FP32, FP16 and BF16 populations sit in 32-cell blocks of 19
+ * slots and FP64 populations in slot rows, both addressed by 32-bit offsets
+ * from one base pointer (faster). The results are the same either way;
+ * lbm_get/set_populations always exchange the reference layout
+ * f[q*n + idx]. */
 #define LBM_FLAG_SLOT_POINTERS 4
 
 typedef struct lbm_solver lbm_solver;

@@ -134,17 +134,18 @@ struct StepArgs {
 //   (row ceil(nx / 32) + x / 32) 19 32 + 32 q + x % 32.
 // A warp (a 32-cell row segment) then finds the 19 slots of its cells at
 // fixed offsets from one base, and its 19 loads fall in one 2.4 kB stretch
-// of HBM (FP32). Storage types whose blocked_layout() holds use it wherever
-// 32-bit offsets reach (19 x the padded cells < 2^32), except under the
-// bulk-copy kernel (which streams slot rows) and LBM_FLAG_SLOT_POINTERS.
-// Measured per C2 launch: FP32 0.1973 -> 0.1931 ms (report steps 0.367 ->
-// 0.355 ms); FP16 0.1498 -> 0.1559 ms in a first form with more spills on
-// the odd step, so 2-byte storage keeps the slot layout.
+// of HBM (FP32; 1.2 kB in FP16/BF16). Storage types whose blocked_layout()
+// holds use it wherever 32-bit offsets reach (19 x the padded cells <
+// 2^32), except under the bulk-copy kernel (which streams slot rows) and
+// LBM_FLAG_SLOT_POINTERS. Measured per C2 launch against the slot layout:
+// FP32 0.1973 -> 0.1931 ms (report steps 0.367 -> 0.355 ms); FP16 0.1505 ->
+// 0.1475 ms, but report steps 0.315 -> 0.333 ms (nine quiet steps and a
+// report: 1.640 -> 1.632 ms). FP64 keeps the slot layout.
 #ifndef LBM_BLOCKED_32
 #define LBM_BLOCKED_32 1
 #endif
 #ifndef LBM_BLOCKED_16
-#define LBM_BLOCKED_16 0
+#define LBM_BLOCKED_16 1
 #endif
 constexpr int BLK = 32;
 __host__ __device__ constexpr bool blocked_layout(int bytes) {

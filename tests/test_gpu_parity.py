@@ -456,18 +456,19 @@ BLOCK_CASES = {
 }
 
 
+@pytest.mark.parametrize("storage", ["f32", "f16", "bf16"])
 @pytest.mark.parametrize("case", list(BLOCK_CASES))
-def test_block_layout_matches_slot_layout(G, case):
-    """FP32 populations in 32-cell blocks (the default layout) and in 19 slot
-    rows (LBM_FLAG_SLOT_POINTERS) go through the same arithmetic, so seven
-    steps (two of them report steps) give bit-identical populations and
-    fields: padded blocks, wrap-around across block edges, lid rows (the
-    general kernel), masked warps."""
+def test_block_layout_matches_slot_layout(G, case, storage):
+    """Populations in 32-cell blocks (the default layout of FP32, FP16 and
+    BF16 storage) and in 19 slot rows (LBM_FLAG_SLOT_POINTERS) go through the
+    same arithmetic, so seven steps (two of them report steps) give
+    bit-identical populations and fields: padded blocks, wrap-around across
+    block edges, lid rows (the general kernel), masked warps."""
     opts = dict(BLOCK_CASES[case])
     nx = opts.pop("nx")
     cfg = O.Config(nx, 12, 7, nu=0.02, u0=0.07, sponge_start=max(nx - 8.0, 0.0), sponge_strength=0.9, **opts)
-    hb = native_handle(cfg, "f32", flags=0)
-    hs = native_handle(cfg, "f32", flags=N.FLAG_SLOT_POINTERS)
+    hb = native_handle(cfg, storage, flags=0)
+    hs = native_handle(cfg, storage, flags=N.FLAG_SLOT_POINTERS)
     for h in (hb, hs):
         h.call("lbm_init_random", 1e-3, 0.01, 11)
     assert np.array_equal(get(hb, cfg.n), get(hs, cfg.n))
