@@ -461,14 +461,18 @@ BLOCK_CASES = {
 def test_block_layout_matches_slot_layout(G, case, storage):
     """Populations in 32-cell blocks (the default layout of FP32, FP16 and
     BF16 storage) and in 19 slot rows (LBM_FLAG_SLOT_POINTERS) go through the
-    same arithmetic, so seven steps (two of them report steps) give
-    bit-identical populations and fields: padded blocks, wrap-around across
-    block edges, lid rows (the general kernel), masked warps."""
+    same arithmetic: over seven steps (two of them report steps) they agree
+    to the parity tolerance, populations and fields, on padded blocks,
+    wrap-around across block edges, lid rows (the general kernel) and masked
+    warps. (The two layouts are separately compiled copies of the step, so
+    the compiler may contract their floating-point expressions differently;
+    an addressing error would show as an O(1) difference.)"""
     opts = dict(BLOCK_CASES[case])
     nx = opts.pop("nx")
     cfg = O.Config(nx, 12, 7, nu=0.02, u0=0.07, sponge_start=max(nx - 8.0, 0.0), sponge_strength=0.9, **opts)
     hb = native_handle(cfg, storage, flags=0)
     hs = native_handle(cfg, storage, flags=N.FLAG_SLOT_POINTERS)
+    tol = {"f32": TOL32, "f16": 4e-4, "bf16": 4e-3}[storage]
     for h in (hb, hs):
         h.call("lbm_init_random", 1e-3, 0.01, 11)
     assert np.array_equal(get(hb, cfg.n), get(hs, cfg.n))
@@ -476,11 +480,10 @@ def test_block_layout_matches_slot_layout(G, case, storage):
         rep = k in (3, 4)
         for h in (hb, hs):
             h.call("lbm_step", int(rep), None)
-        assert np.array_equal(get(hb, cfg.n), get(hs, cfg.n)), f"{case} step {k + 1}"
+        err = O.weight_err(get(hb, cfg.n), get(hs, cfg.n))
+        assert err <= tol, f"{case} step {k + 1}: {err:.3e}"
         if rep:
-            fb, fs = get_fields(hb, cfg.n), get_fields(hs, cfg.n)
-            for name in O.FIELDS:
-                assert np.array_equal(fb[name], fs[name]), f"{case} step {k + 1} {name}"
+            check_fields(get_fields(hb, cfg.n), get_fields(hs, cfg.n), f"{case} step {k + 1}")
 
 
 @pytest.mark.parametrize("kind", ["les_slipz", "lid_box", "heatsink_heat", "bulkcopy", "f16"])
