@@ -1103,36 +1103,37 @@ __device__ __forceinline__ bool lid_row(const StepArgs<S> &a, int y) {
   return a.lateral == SIDE_LID && y == a.ny - 1;
 }
 
-// Resident step_kernel blocks per SM, by storage width. FP32 runs 8 blocks
-// (32 warps, 64 registers) with the odd step's store addresses formed again
-// (opaque_store): 0.203 ms per C2 launch, against 0.206 at 7 blocks,
-// 0.223-0.230 at 6 and 0.225 at 5 (the earlier 5 blocks without
-// opaque_store). FP16/BF16 are latency-bound with half the bytes in flight
-// per warp: with opaque_store and the flat slot offsets 8 blocks (32 warps,
-// 64 registers) run 0.157 ms per C2 launch against 0.162 at 7; without
-// opaque_store 7 blocks were best (0.167; 8: 0.186). FP64 (the oracle-
-// precision runs, twice the registers per value) keeps 5.
+// Resident step_kernel blocks per SM, by storage width, for quiet and report
+// steps. Fewer registers per thread buy resident warps (more loads in
+// flight); the odd step's store addresses are formed again (opaque_store)
+// so that the 19 load addresses need not stay live. Measured per C2 launch
+// (event-timed, 32-cell block layout): FP32 quiet 9 blocks (56 registers)
+// 0.1918 ms against 0.1932 at 8 (64 registers; in slot rows 8 blocks beat 7,
+// 6 and 5: 0.203, 0.206, 0.223-0.230, 0.225); FP32 report steps 0.355 ms at
+// 8 against 0.380 at 9. FP16/BF16 quiet 9 blocks 0.1390 ms against 0.1460
+// at 8 and 0.1639 at 10 (48 registers, heavy spills); FP16 report steps
+// 0.334 ms at 8 against 0.341 at 9. FP64 (the oracle-precision runs, twice
+// the registers per value) keeps 5.
 #ifndef LBM_STEP_MIN_BLOCKS
-#define LBM_STEP_MIN_BLOCKS 8
+#define LBM_STEP_MIN_BLOCKS 9
 #endif
 #ifndef LBM_STEP_MIN_BLOCKS_16
-#define LBM_STEP_MIN_BLOCKS_16 8
+#define LBM_STEP_MIN_BLOCKS_16 9
 #endif
 #ifndef LBM_STEP_MIN_BLOCKS_64
 #define LBM_STEP_MIN_BLOCKS_64 5
 #endif
-// Report steps (13 more field streams and the residuals live) may take their
-// own FP32 block count (0: the quiet one). Measured report steps at C2: 5
-// blocks 0.416 ms, 6 0.395, 7 0.379, 8 (the quiet count) 0.386: within noise
-// of each other from 7 up, so the quiet count is kept.
 #ifndef LBM_STEP_MIN_BLOCKS_REPORT
-#define LBM_STEP_MIN_BLOCKS_REPORT 0
+#define LBM_STEP_MIN_BLOCKS_REPORT 8
+#endif
+#ifndef LBM_STEP_MIN_BLOCKS_REPORT_16
+#define LBM_STEP_MIN_BLOCKS_REPORT_16 8
 #endif
 template <typename S, bool REPORT = false>
 __host__ __device__ constexpr int step_min_blocks() {
-  return REPORT && LBM_STEP_MIN_BLOCKS_REPORT > 0 && sizeof(S) == 4
-             ? LBM_STEP_MIN_BLOCKS_REPORT
-             : sizeof(S) == 2 ? LBM_STEP_MIN_BLOCKS_16 : sizeof(S) == 8 ? LBM_STEP_MIN_BLOCKS_64 : LBM_STEP_MIN_BLOCKS;
+  return sizeof(S) == 8   ? LBM_STEP_MIN_BLOCKS_64
+         : sizeof(S) == 2 ? (REPORT ? LBM_STEP_MIN_BLOCKS_REPORT_16 : LBM_STEP_MIN_BLOCKS_16)
+                          : (REPORT ? LBM_STEP_MIN_BLOCKS_REPORT : LBM_STEP_MIN_BLOCKS);
 }
 
 // One cell of the per-cell kernels: the warp is the 32-cell row segment at x0.
@@ -1169,9 +1170,15 @@ __device__ __forceinline__ void cell_step(const StepArgs<S> &a, int x0, int x, i
 
 // Warps of a step_kernel block along x: 2 for 4-byte storage (a 64 x 2-cell
 // tile, 2 % faster than 32 x 4 in FP32), 1 otherwise (32 x 4 cells).
+#ifndef LBM_TILE_WARPS_X_32
+#define LBM_TILE_WARPS_X_32 2
+#endif
+#ifndef LBM_TILE_WARPS_X_16
+#define LBM_TILE_WARPS_X_16 1
+#endif
 template <typename S>
 __host__ __device__ constexpr int tile_warps_x() {
-  return sizeof(S) == 4 ? 2 : 1;
+  return sizeof(S) == 4 ? LBM_TILE_WARPS_X_32 : sizeof(S) == 2 ? LBM_TILE_WARPS_X_16 : 1;
 }
 
 template <typename S, int COLL, bool REPORT, bool ODD>
