@@ -616,11 +616,17 @@ __device__ __forceinline__ CSum warp_csum(float v) {
 // writes the 8 sums and resets the ticket for the next report step.
 constexpr int SUM_THREADS = 256;
 
+// a + b as an exact pair (Knuth's TwoSum)
+__device__ __forceinline__ CSum two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bp = __fsub_rn(s, a);
+  const float ap = __fsub_rn(s, bp);
+  return {s, __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp))};
+}
+// four values into the running pair: exact pairs of (x, y) and (z, w), their
+// pair sum, then one dependent addition per load instead of four
 __device__ __forceinline__ void csum4(CSum &acc, float4 v) {
-  acc = csum_add(acc, CSum{v.x, 0.f});
-  acc = csum_add(acc, CSum{v.y, 0.f});
-  acc = csum_add(acc, CSum{v.z, 0.f});
-  acc = csum_add(acc, CSum{v.w, 0.f});
+  acc = csum_add(acc, csum_add(two_sum(v.x, v.y), two_sum(v.z, v.w)));
 }
 
 static __global__ void __launch_bounds__(SUM_THREADS)
