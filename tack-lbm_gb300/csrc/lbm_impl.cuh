@@ -130,7 +130,15 @@ cudaError_t launch_variant(const Ctx &c, const StepArgs<S> &a, cudaStream_t st, 
       // the monitor sums, read back from the fields just written
       const int sblocks = (int)std::min<int64_t>((c.n + SUM_THREADS * 16 - 1) / (SUM_THREADS * 16),
                                                  (int64_t)c.num_sms * 8);
-      field_sums_kernel<<<sblocks, SUM_THREADS, 0, st>>>(c.fld_dev, (int)c.n, c.partials, c.ticket, c.sums);
+      SumBox box{};
+      for (int k = 0; k < 3; ++k) {
+        box.lo[k] = c.reach_lo[k];
+        box.hi[k] = c.reach_hi[k];
+      }
+      box.any = c.reach_any;
+      box.nx = c.cfg.nx;
+      box.ny = c.cfg.ny;
+      field_sums_kernel<<<sblocks, SUM_THREADS, 0, st>>>(c.fld_dev, (int)c.n, box, c.partials, c.ticket, c.sums);
       *rows = 0;  // finalized by the kernel's last block
     }
     (void)fblocks;
