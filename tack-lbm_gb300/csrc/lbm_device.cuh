@@ -620,6 +620,11 @@ __device__ __forceinline__ CSum warp_csum(float v) {
 // sums and resets the ticket for the next report step.
 constexpr int SUM_THREADS = 256;
 constexpr int NRES = 5;  // the residual fields, summed over every cell
+// Blocks per SM of field_sums_kernel: its 256 threads of ~60 registers fit 4
+// per SM, so 4 per SM is one wave. With two float4 loads per field in flight
+// per thread: report step 0.339 -> 0.326 ms at C2 (8 per SM, one load: two
+// waves, 0.339; 4 per SM alone 0.333; two loads alone 0.336).
+constexpr int SUM_BLOCKS_PER_SM = 4;
 
 // the cells whose links may reach an obstacle cell (any = 0: none)
 struct SumBox {
@@ -654,7 +659,22 @@ field_sums_kernel(const float *const *fld, int n, SumBox box, float2 *partials, 
   int tail = 0;
   if ((n & 3) == 0) {
     const int n4 = n >> 2;
-    for (int i = (int)blockIdx.x * SUM_THREADS + (int)threadIdx.x; i < n4; i += stride) {
+    int i = (int)blockIdx.x * SUM_THREADS + (int)threadIdx.x;
+    // two loads per field in flight before the additions
+    for (; i + stride < n4; i += 2 * stride) {
+      float4 v[NRES], w[NRES];
+#pragma unroll
+      for (int k = 0; k < NRES; ++k) {
+        v[k] = __ldcs(reinterpret_cast<const float4 *>(f[k]) + i);
+        w[k] = __ldcs(reinterpret_cast<const float4 *>(f[k]) + i + stride);
+      }
+#pragma unroll
+      for (int k = 0; k < NRES; ++k) {
+        csum4(acc[k], v[k]);
+        csum4(acc[k], w[k]);
+      }
+    }
+    for (; i < n4; i += stride) {
       float4 v[NRES];
 #pragma unroll
       for (int k = 0; k < NRES; ++k) v[k] = reinterpret_cast<const float4 *>(f[k])[i];
@@ -827,9 +847,10 @@ __device__ __forceinline__ Offsets<S> cell_offsets(const StepArgs<S> &a, int x, 
 // the whole collision. opaque_store<S>() forms the store addresses again from
 // copies of the cell index and offsets the compiler cannot identify with the
 // originals, which keeps 7 integers live instead. That frees the registers
-// for more blocks per SM (below): FP32 8 blocks, FP16/BF16 8 blocks (at 7
-// blocks the 2-byte kernels ran 3 % slower with it, at 8 6 % faster than the
-// 7 blocks without it). FP64 does not use it.
+// for more blocks per SM (step_min_blocks). In slot rows it made 8 blocks the
+// best count (the 2-byte kernels: 7 blocks 3 % slower with it, 8 blocks 6 %
+// faster than 7 without it); in 32-cell blocks FP16 runs 0.146 ms per C2
+// launch with it and 0.164 without (8 blocks). FP64 does not use it.
 #ifndef LBM_OPAQUE_STORE_16
 #define LBM_OPAQUE_STORE_16 1
 #endif

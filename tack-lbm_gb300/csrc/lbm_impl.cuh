@@ -129,7 +129,7 @@ cudaError_t launch_variant(const Ctx &c, const StepArgs<S> &a, cudaStream_t st, 
     if (REPORT) {
       // the monitor sums, read back from the fields just written
       const int sblocks = (int)std::min<int64_t>((c.n + SUM_THREADS * 16 - 1) / (SUM_THREADS * 16),
-                                                 (int64_t)c.num_sms * 8);
+                                                 (int64_t)c.num_sms * SUM_BLOCKS_PER_SM);
       SumBox box{};
       for (int k = 0; k < 3; ++k) {
         box.lo[k] = c.reach_lo[k];
