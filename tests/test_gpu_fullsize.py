@@ -6,6 +6,9 @@ the oracle to step the whole lattice:
 * two full C2 steps against the oracle on a sample of cells: every cell that
   bounces back, the slip walls, the sponge and a random draw of the interior,
   to |df|/w_q <= 1e-6 in FP32 and the storage quantum in FP16/BF16;
+* the block layout past 2^31 elements: on a 512x256x880 lattice (19 x 115M
+  positions, periodic z whose wrap offset passes 2^31) four steps in 32-cell
+  blocks agree with the same steps in slot rows, fields and monitor sums;
 * mass over 200 steps of a C2-sized lattice with a static cylinder, periodic
   boundaries and no sponge. Streaming and bounce-back conserve mass, but the
   collision does not quite: the reference uploads float32 lattice weights
@@ -85,6 +88,48 @@ def test_c2_steps_on_sampled_cells(storage, tol):
         want = O.step(cfg, f_in, cells=sample)
         err = (np.abs(f_out[:, sample] - want) / O.W[:, None]).max()
         assert err <= tol, (storage, k + 1, err)
+
+
+def test_block_layout_past_2_31_elements():
+    """Positions in the block layout pass 2^31 above z = 440 here and the
+    periodic z wrap offsets are 2^31 < (nz - 1) plane < 2^32, so every
+    position and offset sum runs modulo 2^32. FP16 storage (4.4 GB per
+    solver); the slot-row solver (LBM_FLAG_SLOT_POINTERS) is the check."""
+    import ctypes
+    import lbm_native as N
+    from test_gpu_parity import native_handle
+    cfg = O.Config(512, 256, 880, collision="les", nu=0.08 * 32 / 300, obstacle="cylinder", ox=128.0,
+                   oy=128.0, r=16.0, u0=0.08, sponge_start=480.0, sponge_strength=1.0, lateral="slip",
+                   vertical="periodic")
+    assert 19 * cfg.n > 2 ** 31 and 19 * (cfg.nz - 1) * cfg.nx * cfg.ny > 2 ** 31
+    sums = {}
+    fields = {}
+    for flags in (0, N.FLAG_SLOT_POINTERS):
+        h = native_handle(cfg, "f16", flags=flags)
+        h.call("lbm_init_random", 1e-3, 1e-3, 29)
+        for k in range(4):
+            h.call("lbm_step", int(k in (1, 3)), None)
+        out = (ctypes.c_double * 8)()
+        h.call("lbm_field_sums", out)
+        sums[flags] = np.array(out)
+        h.call("lbm_sync")
+        fields[flags] = {}
+        for name in ("ux", "uy", "uz", "p", "fx", "r_ux"):
+            ptr = ctypes.c_void_p()
+            h.call("lbm_field", O.FIELDS.index(name), ctypes.byref(ptr))
+            fields[flags][name] = np.ctypeslib.as_array((ctypes.c_float * cfg.n).from_address(ptr.value)).copy()
+        del h
+    blk, slots = fields[0], fields[N.FLAG_SLOT_POINTERS]
+    # an addressing error moves populations between cells: O(1e-2) in u, O(1e-3) in f
+    for name in blk:
+        err = np.abs(blk[name].astype(np.float64) - slots[name]).max()
+        assert err <= 1e-5, (name, err)
+    # the upper half of the lattice (positions past 2^31) is live flow, not zeros
+    upper = blk["ux"][cfg.n // 2:]
+    assert np.isfinite(upper).all() and np.abs(upper).mean() > 0.05
+    # drag, lift and side force sums (the residual sums are squares of
+    # differences between report steps, too sensitive to compare across builds)
+    np.testing.assert_allclose(sums[0][5:], sums[N.FLAG_SLOT_POINTERS][5:], rtol=1e-4, atol=1e-9)
 
 
 def test_c2_sized_mass_follows_the_float32_weights():
