@@ -59,8 +59,18 @@ __device__ __forceinline__ int heat_mask_slot(const HeatArgs &h, int x0, int y, 
   return (((z - h.reach_lo[2]) * nyr + (y - h.reach_lo[1])) * nw + (x0 / BX - w0)) * BX;
 }
 
-// One cell per thread; a warp is a 32-cell row segment (block 32 x 8).
-template <bool REPORT>
+// Slot q of cell e in an A/B temperature buffer: FLAT (7 n < 2^32) forms a
+// 32-bit element offset from the base, else a 64-bit one.
+template <bool FLAT, typename P>
+__device__ __forceinline__ P *heat_at(P *g, const HeatArgs &h, int q, int e) {
+  if (FLAT) return g + (uint32_t)((uint32_t)q * (uint32_t)h.n + (uint32_t)e);
+  return g + (size_t)q * h.n + e;
+}
+
+// One cell per thread; a warp is a 32-cell row segment (block 32 x 8). The
+// sources come from six per-cell neighbour offsets; their coordinates are
+// formed only where a wall or sink test needs them.
+template <bool REPORT, bool FLAT>
 __global__ void __launch_bounds__(256) heat_kernel(const __grid_constant__ HeatArgs h) {
   const int x0 = (int)blockIdx.x * BX, x = x0 + (int)threadIdx.x;
   const int y = (int)blockIdx.y * blockDim.y + (int)threadIdx.y, z = (int)blockIdx.z;
@@ -76,23 +86,44 @@ __global__ void __launch_bounds__(256) heat_kernel(const __grid_constant__ HeatA
   const float fluid = here ? 0.f : 1.f;
   float g[7], temp = 0.f;
   int src[7];
+  const int nxy = h.nx * h.ny;
+  const int dxm = x == 0 ? h.nx - 1 : -1, dxp = x == h.nx - 1 ? 1 - h.nx : 1;
+  const int dym = y == 0 ? nxy - h.nx : -h.nx, dyp = y == h.ny - 1 ? h.nx - nxy : h.nx;
+  const int dzm = z == 0 ? (h.nz - 1) * nxy : -nxy, dzp = z == h.nz - 1 ? -(h.nz - 1) * nxy : nxy;
   static_for<7>([&](auto qc) {
     constexpr int q = decltype(qc)::value;
-    int xs = x - cx7(q), ys = y - cy7(q), zs = z - cz7(q);
-    xs += xs < 0 ? h.nx : 0;
-    xs -= xs >= h.nx ? h.nx : 0;
-    ys += ys < 0 ? h.ny : 0;
-    ys -= ys >= h.ny ? h.ny : 0;
-    zs += zs < 0 ? h.nz : 0;
-    zs -= zs >= h.nz ? h.nz : 0;
-    const int nidx = (zs * h.ny + ys) * h.nx + xs;
+    // the source x - c_q, periodic in all three axes
+    const int nidx = idx + (cx7(q) == 1 ? dxm : cx7(q) == -1 ? dxp : 0) +
+                     (cy7(q) == 1 ? dym : cy7(q) == -1 ? dyp : 0) + (cz7(q) == 1 ? dzm : cz7(q) == -1 ? dzp : 0);
+    auto coords = [&](int &xs, int &ys, int &zs) {
+      xs = x - cx7(q);
+      ys = y - cy7(q);
+      zs = z - cz7(q);
+      xs += xs < 0 ? h.nx : 0;
+      xs -= xs >= h.nx ? h.nx : 0;
+      ys += ys < 0 ? h.ny : 0;
+      ys -= ys >= h.ny ? h.ny : 0;
+      zs += zs < 0 ? h.nz : 0;
+      zs -= zs >= h.nz ? h.nz : 0;
+    };
     src[q] = nidx;
-    const float pulled = load_l2(h.g_in + (size_t)q * h.n + nidx);
+    const float pulled = load_l2(heat_at<FLAT>(h.g_in, h, q, nidx));
     float val = pulled;
     // D3Q7 direction q (1..6) is D3Q19 direction q: the same link-mask bit
-    const bool wall = q != 0 && (h.use_masks ? ((m >> q) & 1u) != 0 : solid(h.geo, xs, ys, zs));
+    bool wall = false;
+    if (q != 0) {
+      if (h.use_masks) {
+        wall = ((m >> q) & 1u) != 0;
+      } else {
+        int xs, ys, zs;
+        coords(xs, ys, zs);
+        wall = solid(h.geo, xs, ys, zs);
+      }
+    }
     if (wall) {
-      const float bounced = h.g_in[(size_t)opp7(q) * h.n + idx];
+      int xs, ys, zs;
+      coords(xs, ys, zs);
+      const float bounced = *heat_at<FLAT>(h.g_in, h, opp7(q), idx);
       val = sink(h.geo, xs, ys, zs) ? -bounced + 2.0f * w7(q) * h.t_solid[nidx] : bounced;
     }
     g[q] = val;
@@ -118,7 +149,7 @@ __global__ void __launch_bounds__(256) heat_kernel(const __grid_constant__ HeatA
     const float eq = w7(q) * temp * (1.f + 4.f * ((float)cx7(q) * ux + (float)cy7(q) * uy + (float)cz7(q) * uz));
     const float post = g[q] - om * (g[q] - eq);
     const float es = w7(q) * temp_s * (1.f + 4.f * ((float)cx7(q) * usx + (float)cy7(q) * usy + (float)cz7(q) * usz));
-    __stcs(h.g_out + (size_t)q * h.n + idx, es + keep * (post - eq));
+    __stcs(heat_at<FLAT>(h.g_out, h, q, idx), es + keep * (post - eq));
   });
   if (REPORT) {
     h.temp[idx] = here ? h.t_solid[idx] : temp;
@@ -169,11 +200,14 @@ cudaError_t launch_heat(const Ctx &c, bool report, cudaStream_t st) {
   h.use_masks = g.lateral == LBM_PERIODIC && g.vertical == LBM_PERIODIC && (!c.reach_any || c.wmasks) ? 1 : 0;
   const dim3 block(lbmk::BX, 8);
   const dim3 grid((g.nx + lbmk::BX - 1) / lbmk::BX, (g.ny + 7) / 8, g.nz);
+  const bool flat = 7 * c.n <= (int64_t)UINT32_MAX;
   if (report) {
     cudaMemsetAsync(c.heat_fld[LBM_Q_SOLID], 0, (size_t)c.n * sizeof(float), st);
-    lbmk::heat_kernel<true><<<grid, block, 0, st>>>(h);
+    if (flat) lbmk::heat_kernel<true, true><<<grid, block, 0, st>>>(h);
+    else lbmk::heat_kernel<true, false><<<grid, block, 0, st>>>(h);
   } else {
-    lbmk::heat_kernel<false><<<grid, block, 0, st>>>(h);
+    if (flat) lbmk::heat_kernel<false, true><<<grid, block, 0, st>>>(h);
+    else lbmk::heat_kernel<false, false><<<grid, block, 0, st>>>(h);
   }
   return cudaGetLastError();
 }
